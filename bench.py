@@ -1,0 +1,369 @@
+"""Benchmark of the nonlinear ray-casting hot path.
+
+Headline workload (one "step"): the Cornell room at 1920x1080, one ray per
+pixel, three field functions rendered in turn (linear, twist, point lens),
+RK4 h = 0.005 for 4000 steps with Kahan-compensated position and time, FP32.
+Metric: RK4 ray-steps per second (accepted steps summed over all rays of the
+step / device time), plus ms per 1080p frame.  Inputs are resident (scene,
+compiled fields); L2 is flushed (256 MB write) between timed steps, outside
+the timed events.
+
+Also reported: `e2e` (the same metric through the C-ABI host call
+linon_render_host, device->host copies of all output planes inside the timed
+region), the batched persistent kernel vs the plain per-view kernel on the
+64-view uneven workload, the FP32 roofline of the march kernel against a
+measured FFMA peak, and the oracle's CPU throughput on a bounded sample.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "RK4 ray-steps/s (1920x1080, 3 fields x 4000 steps)"
+UNIT = "ray-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def flops_per_step(wl_mod, pyoracle, w, fid):
+    """Algorithmic FP32 operations of one accepted RK4 step (field evaluations,
+    RK4 bookkeeping, blend, Kahan sums), counted by the oracle's counting
+    float on an empty scene (intersection work excluded: the BVH culls it and
+    brute-force-equivalent FLOPs are not claimed)."""
+    import numpy as _np
+    pix = _np.array([w.width // 2 + (w.height // 2) * w.width, 17 + 11 * w.width], _np.int32)
+    p = wl_mod.fixed_steps(w.params.h_initial, 64, kahan=bool(w.params.kahan))
+    ops, steps = pyoracle.count_ops(_np.zeros((0, 3), _np.float32), _np.zeros((0, 3), _np.uint32), w.camera,
+                                    w.settings, p, fid, w.width, w.height, pix)
+    arith = (ops[:, 0] + ops[:, 1] + ops[:, 2] + ops[:, 3]).astype(float) / steps
+    transc = ops[:, 5].astype(float) / steps
+    return float(arith.mean()), float(transc.mean())
+
+
+def cpu_baseline(pyoracle, w, budget_s=12.0):
+    """The oracle (FP32 restatement) on the host cores over a stratified
+    pixel sample of the same frames; returns ray-steps/s and the sample."""
+    threads = pyoracle.max_threads()
+    rng = np.random.default_rng(0)
+    n_total = w.width * w.height
+    # calibrate on a small sample, then size the measured sample to the budget
+    pix = np.sort(rng.choice(n_total, size=256, replace=False)).astype(np.int32)
+    t0 = time.perf_counter()
+    steps = 0
+    for fid in w.fields:
+        r = pyoracle.render(w.xyz, w.faces, w.face_rgb, w.camera, w.settings, w.params, fid, w.width, w.height,
+                            pixels=pix, threads=threads, want=("steps",))
+        steps += int(r["steps"].sum())
+    dt = time.perf_counter() - t0
+    n = int(min(n_total, max(256, 256 * budget_s / max(dt, 1e-3) * 0.8)))
+    pix = np.sort(rng.choice(n_total, size=n, replace=False)).astype(np.int32)
+    t0 = time.perf_counter()
+    steps = 0
+    for fid in w.fields:
+        r = pyoracle.render(w.xyz, w.faces, w.face_rgb, w.camera, w.settings, w.params, fid, w.width, w.height,
+                            pixels=pix, threads=threads, want=("steps",))
+        steps += int(r["steps"].sum())
+    dt = time.perf_counter() - t0
+    return steps / dt, threads, f"{n} of {n_total} pixels (uniform random, seed 0) x {len(w.fields)} fields, {dt:.1f} s"
+
+
+def run_reference(args):
+    """--impl reference: the reference path's CPU implementation on the host
+    cores.  The reference is WGSL run through wgpu on a graphics API, which
+    does not exist on this machine, so its CPU path is the oracle port (the
+    FP32 restatement of the shader, OpenMP over all host threads)."""
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    from linon_gb300 import workloads as wl
+    from oracle import pyoracle
+    w = wl.frames_1080p(args.width, args.height)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, threads, sample = cpu_baseline(pyoracle, w, budget_s=6.0 if i >= args.warmup else 2.0)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w.name, "width": w.width, "height": w.height, "fields": ["linear", "twist", "lens"],
+                       "h": 0.005, "steps_per_ray": 4000, "kahan": True},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    import torch.distributed as dist
+
+    from linon_gb300 import Engine, FramePlanes, workloads as wl
+    from linon_gb300.engine import predefined_source
+    from oracle import pyoracle
+
+    rank, world, local = dist_info()
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    os.environ.setdefault("LINON_CACHE_DIR", str(ROOT / "_build_cache"))
+    Path(os.environ["LINON_CACHE_DIR"]).mkdir(exist_ok=True)
+
+    w = wl.frames_1080p(args.width, args.height)
+    eng = Engine(local)
+    stream = torch.cuda.Stream(device=dev)
+    eng.set_stream(stream)
+    eng.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    fields = [eng.compile_field(predefined_source(fid)) for fid in w.fields]
+    planes = [FramePlanes.allocate(w.width, w.height, dev) for _ in fields]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step():
+        for f, p in zip(fields, planes):
+            eng.render(f, w.camera, w.settings, w.params, p)
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(3, args.warmup)):
+            step()
+        stream.synchronize()
+        eng.synchronize()
+        steps_per_frame = [int(p.steps.sum().item()) for p in planes]
+    ray_steps = sum(steps_per_frame)
+
+    # ---- timed region: device time of exactly K steps (events on the
+    #      engine's stream), L2 flushed between steps outside the events ----
+    clocks = ClockSampler(torch.cuda.current_device())
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    fev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in fields]
+           for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            evs[k][0].record(stream)
+            for i, (f, p) in enumerate(zip(fields, planes)):
+                fev[k][i][0].record(stream)
+                eng.render(f, w.camera, w.settings, w.params, p)
+                fev[k][i][1].record(stream)
+            evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    eng.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = sum(step_ms)
+    frame_ms = [[a.elapsed_time(b) for a, b in row] for row in fev]
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = ray_steps * args.steps * world / (total_ms * 1e-3)
+    ms_per_step = total_ms / args.steps
+    per_field_ms = [statistics.median(col) for col in zip(*frame_ms)]
+
+    # ---- e2e: the reference-facing C-ABI call with host output buffers ----
+    n_pix = w.width * w.height
+    host = [{"color": torch.empty((w.height, w.width, 4), dtype=torch.uint8).pin_memory().numpy(),
+             "mapping": torch.empty((w.height, w.width, 4), dtype=torch.float32).pin_memory().numpy(),
+             "hit_id": torch.empty((w.height, w.width), dtype=torch.int32).pin_memory().numpy(),
+             "steps": torch.empty((w.height, w.width), dtype=torch.int32).pin_memory().numpy()} for _ in fields]
+    for f, h in zip(fields, host):  # warm the host-path buffers
+        eng.render_host(f, w.camera, w.settings, w.params, w.width, w.height, **h)
+    e2e_steps = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for f, h in zip(fields, host):
+            eng.render_host(f, w.camera, w.settings, w.params, w.width, w.height, **h)
+            e2e_steps += int(h["steps"].sum(dtype=np.int64))
+    e2e_dt = time.perf_counter() - t0
+    e2e = {"value": e2e_steps / e2e_dt * world, "unit": UNIT,
+           "h2d_bytes_per_step": len(fields) * (112 + 24 + 48),
+           "d2h_bytes_per_step": len(fields) * n_pix * (4 + 16 + 4 + 4),
+           "path": "linon_render_host (C ABI), host planes copied back inside the call"}
+
+    result = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+              "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+              "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene and cameras)",
+              "config": {"workload": w.name, "width": w.width, "height": w.height,
+                         "fields": ["linear", "twist", "lens"], "h": 0.005, "steps_per_ray": 4000,
+                         "kahan": True, "bvh": True, "l2": "flushed between steps (256 MB write, outside events)",
+                         "parallelism": f"replicas x{world}"},
+              "frame_ms_1080p": {n: round(v, 3) for n, v in zip(["linear", "twist", "lens"], per_field_ms)},
+              "wall_s_timed_region": wall, "e2e": e2e, "clocks": clk,
+              "gpu_launches": args.steps * len(fields)}
+
+    # ---- roofline: FP32 against a measured FFMA peak ----
+    if rank == 0:
+        peak = eng.probe_fp32_peak()
+        fl = [flops_per_step(wl, pyoracle, w, fid) for fid in w.fields]
+        # dominant kernel: the march launch with the largest median time
+        i = int(np.argmax(per_field_ms))
+        achieved = fl[i][0] * steps_per_frame[i] / (per_field_ms[i] * 1e-3) / 1e12
+        traffic = None
+        tfile = ROOT / "profiles" / "march_traffic.json"
+        if tfile.exists():
+            try:
+                traffic = json.loads(tfile.read_text()).get(["linear", "twist", "lens"][i])
+            except Exception:
+                traffic = None
+        result["roofline"] = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                              "frac": achieved / peak, "traffic": traffic,
+                              "kernel": f"linon_march_a0_k1 ({['linear', 'twist', 'lens'][i]} field)",
+                              "peak_source": "measured FFMA probe in this run (linon_probe_fp32_peak)",
+                              "flops_per_step": {n: round(a, 2) for n, (a, _) in zip(["linear", "twist", "lens"], fl)},
+                              "transcendentals_per_step": {n: round(t, 2) for n, (_, t) in
+                                                           zip(["linear", "twist", "lens"], fl)},
+                              "all_fields_frac": sum(a * s for (a, _), s in zip(fl, steps_per_frame))
+                              / (sum(per_field_ms) * 1e-3) / 1e12 / peak}
+
+    # ---- batched persistent kernel vs plain per-view kernel (64 views) ----
+    if rank == 0 and not args.no_batch:
+        result["batch_uneven_64"] = bench_batch(eng, stream, wl, torch, dev, predefined_source)
+
+    # ---- CPU baseline (oracle port on this host's cores, bounded sample) ----
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, threads, sample = cpu_baseline(pyoracle, w)
+        result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(result))
+    eng.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def bench_batch(eng, stream, wl, torch, dev, predefined_source):
+    from linon_gb300 import FramePlanes, _abi
+    w = wl.batch_uneven(64, seed=0)
+    eng.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    flds = [eng.compile_field(predefined_source(fid)) for fid in w.fields]
+    views, planes = [], []
+    for (W, H, camera, params, fidx) in w.extra["views"]:
+        p = FramePlanes.allocate(W, H, dev)
+        v = _abi.View()
+        v.camera, v.settings, v.params = camera, wl.settings(), params
+        v.width, v.height, v.field_index = W, H, fidx
+        v.out = p.abi()
+        views.append(v)
+        planes.append(p)
+
+    def timed(fn, reps=3):
+        ts = []
+        with torch.cuda.stream(stream):
+            fn()
+            stream.synchronize()
+            for _ in range(reps):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fn()
+                b.record(stream)
+                b.synchronize()
+                ts.append(a.elapsed_time(b))
+        return statistics.median(ts)
+
+    plain_ms = timed(lambda: eng.render_views_plain(flds, views))
+    steps_plain = sum(int(p.steps.sum().item()) for p in planes)
+    tuning, tune_ms = eng.autotune_batch(flds, views)
+    batch_ms = timed(lambda: eng.render_batch(flds, views, tuning))
+    eng.synchronize()
+    steps_batch = sum(int(p.steps.sum().item()) for p in planes)
+    rays = sum(v.width * v.height for v in views)
+    return {"views": len(views), "rays": rays, "ray_steps": steps_batch, "plain_ms": plain_ms,
+            "batched_ms": batch_ms, "plain_ray_steps_per_s": steps_plain / (plain_ms * 1e-3),
+            "batched_ray_steps_per_s": steps_batch / (batch_ms * 1e-3), "speedup": plain_ms / batch_ms,
+            "tuning": {"quantum": tuning.quantum, "block_threads": tuning.block_threads,
+                       "tile": [tuning.tile_w, tuning.tile_h]}}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,611 @@
+// march.cuh — nonlinear ray-casting kernels (device code compiled by NVRTC
+// together with the CUDA C that the WGSL front end generated for the field
+// functions).
+//
+// Reference: src/main_view.wgsl
+//   :339-376 main_view  (primary ray per pixel, stores)
+//   :229-279 nonlinear_ray_color (RK4, adaptive step, first-hit colour,
+//            endpoint "mapping")
+//   :177-220 ray_color, :150-175 hit_triangle (Moeller-Trumbore)
+//   :281-314 sample_rays, :470-479 capture seeds
+// Every arithmetic expression keeps the shader's evaluation order, so a
+// module compiled with LINON_PRECISE and --fmad=false is op-for-op the FP32
+// restatement.  Fast modules let the compiler contract a*b+c into FMA and use
+// the hardware reciprocal square root.
+#pragma once
+
+#include "wgsl_rt.cuh"
+#include "march_types.h"
+
+namespace linon {
+
+using wgsl::vec3f;
+
+#if defined(LINON_PRECISE)
+#define LINON_DIV6(x) ((x) / 6.0f)
+#else
+#define LINON_DIV6(x) ((x) * (1.0f / 6.0f))
+#endif
+
+// --------------------------------------------------------------------------
+// Scene access.  Triangles are three float4 each: (v0, face id bits),
+// (e1 = v1 - v0, 0), (e2 = v2 - v0, 0); e1/e2 are the differences
+// hit_triangle computes (IEEE subtraction, so precomputing them changes
+// nothing).  BVH nodes are two float4: (lo.xyz, first), (hi.xyz, count);
+// count > 0 is a leaf over triangles [first, first+count), otherwise the
+// children are nodes first and first+1.  Node boxes are inflated on the host
+// so that culling never drops a triangle the brute-force loop would hit.
+// --------------------------------------------------------------------------
+struct SceneView {
+  const float4* tris;
+  const float4* nodes;
+  const float4* face_rgb;
+  int n_tris;
+  int n_nodes;
+};
+
+__device__ __forceinline__ vec3f xyz(const float4& a) { return vec3f(a.x, a.y, a.z); }
+
+// hit_triangle, main_view.wgsl:150-175 (eps 1e-7, no back-face culling)
+__device__ __forceinline__ float hit_triangle(const vec3f& v0, const vec3f& edge1,
+                                              const vec3f& edge2, const vec3f& origin,
+                                              const vec3f& direction) {
+  const float eps = 1e-7f;
+  vec3f h = wgsl::cross(direction, edge2);
+  float a = wgsl::dot(edge1, h);
+  if (a > -eps && a < eps) return -1.0f;
+  float f = 1.0f / a;
+  vec3f s = origin - v0;
+  float u = f * wgsl::dot(s, h);
+  if (u < 0.0f || u > 1.0f) return -1.0f;
+  vec3f q = wgsl::cross(s, edge1);
+  float v = f * wgsl::dot(direction, q);
+  if (v < 0.0f || u + v > 1.0f) return -1.0f;
+  float t = f * wgsl::dot(edge2, q);
+  if (t > eps) return t;
+  return -1.0f;
+}
+
+struct HitRec {
+  float t;   // -1: none
+  int id;    // original face index
+  int slot;  // position in the triangle array
+};
+
+// Closest hit of the segment origin + [0, max_dist) * direction, ties to the
+// lower face index (the brute-force loop's strict `<`, main_view.wgsl:193).
+__device__ __forceinline__ void test_tri(const SceneView& sc, int slot, const vec3f& origin,
+                                         const vec3f& direction, float max_dist, HitRec& best) {
+  const float4 A = sc.tris[3 * slot];
+  const float4 B = sc.tris[3 * slot + 1];
+  const float4 C = sc.tris[3 * slot + 2];
+  float t_new = hit_triangle(xyz(A), xyz(B), xyz(C), origin, direction);
+  if (t_new > 0.0f && t_new < max_dist) {
+    int id = __float_as_int(A.w);
+    if (best.t < 0.0f || t_new < best.t || (t_new == best.t && id < best.id)) {
+      best.t = t_new;
+      best.id = id;
+      best.slot = slot;
+    }
+  }
+}
+
+__device__ __forceinline__ bool box_overlap(const float4& lo, const float4& hi, const vec3f& smin,
+                                            const vec3f& smax) {
+  return !(smax.x < lo.x || smin.x > hi.x || smax.y < lo.y || smin.y > hi.y || smax.z < lo.z ||
+           smin.z > hi.z);
+}
+
+#ifndef LINON_BVH_STACK
+#define LINON_BVH_STACK 48
+#endif
+
+// Segment query; seg_end is origin + step (the unnormalised step vector).
+__device__ __forceinline__ HitRec intersect_segment(const SceneView& sc, const vec3f& origin,
+                                                    const vec3f& direction, float max_dist,
+                                                    const vec3f& seg_end, int* err) {
+  HitRec best;
+  best.t = -1.0f;
+  best.id = 0x7fffffff;
+  best.slot = -1;
+  if (sc.n_nodes == 0) {
+    for (int i = 0; i < sc.n_tris; ++i) test_tri(sc, i, origin, direction, max_dist, best);
+    return best;
+  }
+  vec3f smin = wgsl::min(origin, seg_end), smax = wgsl::max(origin, seg_end);
+  int stack[LINON_BVH_STACK];
+  int sp = 0;
+  int node = 0;
+  for (;;) {
+    const float4 lo = sc.nodes[2 * node];
+    const float4 hi = sc.nodes[2 * node + 1];
+    bool visit = box_overlap(lo, hi, smin, smax);
+    if (visit) {
+      int first = __float_as_int(lo.w);
+      int count = __float_as_int(hi.w);
+      if (count > 0) {
+        for (int i = 0; i < count; ++i) test_tri(sc, first + i, origin, direction, max_dist, best);
+      } else {
+        if (sp < LINON_BVH_STACK) {
+          stack[sp++] = first + 1;
+        } else {
+          // The host caps the tree depth below the stack size, so this is
+          // unreachable; if it ever were reached the flag reports it.
+          atomicOr(err, 2);
+        }
+        node = first;
+        continue;
+      }
+    }
+    if (sp == 0) break;
+    node = stack[--sp];
+  }
+  return best;
+}
+
+// Shading of ray_color, main_view.wgsl:199-217 (camera is the light source).
+__device__ __forceinline__ wgsl::vec4f shade_hit(const SceneView& sc, const HitRec& hit,
+                                                 const vec3f& direction) {
+  const vec3f d1 = xyz(sc.tris[3 * hit.slot + 1]);
+  const vec3f d2 = xyz(sc.tris[3 * hit.slot + 2]);
+  vec3f normal = wgsl::normalize(wgsl::cross(d1, d2));
+  float intensity = wgsl::max(wgsl::dot(normal, -direction), 0.0f);
+  if (intensity == 0.0f) intensity = wgsl::max(wgsl::dot(-normal, -direction), 0.0f);
+  float spec = powf(intensity, 64.0f);
+  float shade = (0.01f + intensity) + spec;
+  vec3f base = wgsl::abs(normal);
+  if (sc.face_rgb) {
+    const float4 c = sc.face_rgb[hit.id];
+    base = vec3f(c.x, c.y, c.z);
+  }
+  return wgsl::vec4f(shade * base.x, shade * base.y, shade * base.z, hit.t);
+}
+
+// --------------------------------------------------------------------------
+// Camera, main_view.wgsl:347-366
+// --------------------------------------------------------------------------
+struct Basis {
+  vec3f origin, view_direction, nh, nv;
+  float width, height, vw, vh, focal;
+};
+
+__device__ __forceinline__ Basis make_basis(const DevCamera& c, int W, int H, float focal,
+                                            float viewport_height) {
+  Basis b;
+  b.width = float(W);
+  b.height = float(H);
+  float aspect = b.width / b.height;
+  b.origin = vec3f(c.o[0], c.o[1], c.o[2]);
+  b.view_direction = vec3f(c.d[0], c.d[1], c.d[2]);
+  vec3f up(c.u[0], c.u[1], c.u[2]);
+  b.focal = focal;
+  b.vh = viewport_height;
+  b.vw = aspect * b.vh;
+  vec3f w = -b.view_direction;
+  vec3f horizontal = wgsl::cross(up, w);
+  vec3f vertical = wgsl::cross(w, horizontal);
+  b.nh = wgsl::normalize(horizontal);
+  b.nv = wgsl::normalize(vertical);
+  return b;
+}
+
+__device__ __forceinline__ vec3f primary_dir(const Basis& b, int gx, int gy) {
+  float u = float(gx) / (b.width - 1.0f) * b.vw - 0.5f * b.vw;
+  float v = float(gy) / (b.height - 1.0f) * b.vh - 0.5f * b.vh;
+  vec3f s = (u * b.nh + v * b.nv) + b.focal * b.view_direction;
+  return wgsl::normalize(s);
+}
+
+__device__ __forceinline__ vec3f position_dir(const Basis& b, float px, float py) {
+  float u2 = px * b.vw - 0.5f * b.vw;
+  float v2 = py * b.vh - 0.5f * b.vh;
+  vec3f s2 = (u2 * b.nh + v2 * b.nv) + b.focal * b.view_direction;
+  return wgsl::normalize(s2);
+}
+
+__device__ __forceinline__ unsigned char unorm8(float x) {
+  float c = fminf(fmaxf(x, 0.0f), 1.0f);
+  return (unsigned char)__float2uint_rn(c * 255.0f);
+}
+
+// --------------------------------------------------------------------------
+// Ray state and the RK4 march
+// --------------------------------------------------------------------------
+struct RayState {
+  vec3f p, dir, v0;     // position, direction, start direction
+  vec3f last_v;
+  vec3f cp;             // Kahan carry of p
+  float t, ct;          // time and its Kahan carry
+  float h, last_diff;
+  wgsl::vec4f color;
+  int face;
+  int steps;
+  bool has_color;
+};
+
+__device__ __forceinline__ void ray_init(RayState& r, const vec3f& origin, const vec3f& dir,
+                                         float h_initial) {
+  r.p = origin;
+  r.dir = dir;
+  r.v0 = dir;
+  r.last_v = vec3f(0.0f, 0.0f, 0.0f);
+  r.cp = vec3f(0.0f, 0.0f, 0.0f);
+  r.t = 0.0f;
+  r.ct = 0.0f;
+  r.h = h_initial;
+  r.last_diff = -1.0f;
+  r.color = wgsl::vec4f(0.0f, 0.0f, 0.0f, 0.0f);
+  r.face = -1;
+  r.steps = 0;
+  r.has_color = false;
+}
+
+__device__ __forceinline__ void kahan_add(float& sum, float& c, float x) {
+  float y = x - c;
+  float t = sum + y;
+  c = (t - sum) - y;
+  sum = t;
+}
+
+// Is the ray still marching?  (loop condition of main_view.wgsl:244, or the
+// fixed step budget, or the first hit with stop_on_hit)
+__device__ __forceinline__ bool ray_active(const RayState& r, const DevMarch& m) {
+  if (m.stop_on_hit && r.has_color) return false;
+  if (m.max_steps > 0) return r.steps < m.max_steps;
+  return r.t <= m.t_max;
+}
+
+// One attempted RK4 step (main_view.wgsl:245-270).  Returns false when the
+// step was rejected by the adaptive rule (h refined, nothing advanced).
+template <bool ADAPTIVE, bool KAHAN, class F>
+__device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevMarch& m,
+                                         const SceneView& sc, int* err) {
+  const float h = r.h;
+  const float hh = 0.5f * h;
+  const vec3f k1 = field(r.p, r.p, r.v0, r.dir, r.t);
+  const vec3f k2 = field(r.p, r.p + hh * k1, r.v0, k1, r.t + hh);
+  const vec3f k3 = field(r.p, r.p + hh * k2, r.v0, k2, r.t + hh);
+  const vec3f k4 = field(r.p, r.p + h * k3, r.v0, k3, r.t + h);
+  const vec3f v = LINON_DIV6(((k1 + 2.0f * k2) + 2.0f * k3) + k4);
+  float diff = 0.0f;
+  if (ADAPTIVE) {
+    diff = wgsl::length(v - r.last_v);
+    if (r.last_diff >= 0.0f && diff > 10.0f * r.last_diff && h > m.h_fine_above) {
+      r.h = m.h_fine;
+      return false;
+    }
+  }
+  const float w = m.field_weight;
+  r.dir = (1.0f - w) * r.dir + w * v;
+  const vec3f step_dir = r.dir * h;
+  if (!r.has_color) {
+    const float len = wgsl::length(step_dir);
+#if defined(LINON_PRECISE)
+    const vec3f dirn = step_dir / len;
+#else
+    const vec3f dirn = wgsl::normalize(step_dir);
+#endif
+    HitRec hit = intersect_segment(sc, r.p, dirn, len, r.p + step_dir, err);
+    if (hit.t > 0.0f && hit.t < len) {
+      r.color = shade_hit(sc, hit, dirn);
+      r.has_color = r.color.w > 0.0f;
+      if (r.has_color) r.face = hit.id;
+    }
+  }
+  if (KAHAN) {
+    kahan_add(r.p.x, r.cp.x, step_dir.x);
+    kahan_add(r.p.y, r.cp.y, step_dir.y);
+    kahan_add(r.p.z, r.cp.z, step_dir.z);
+    kahan_add(r.t, r.ct, h);
+  } else {
+    r.p = r.p + step_dir;
+    r.t = r.t + h;
+  }
+  if (ADAPTIVE) {
+    r.last_v = v;
+    if (2.0f * diff < r.last_diff && h < m.h_initial) r.h = m.h_initial;
+    r.last_diff = diff;
+  }
+  r.steps++;
+  return true;
+}
+
+// Final stores of main_view.wgsl:373-374 (alpha forced to 1, wgsl:274-277).
+__device__ __forceinline__ void ray_store(const RayState& r, const DevFrame& f, size_t idx) {
+  if (f.color) {
+    uchar4 c;
+    if (r.has_color) {
+      c.x = unorm8(r.color.x);
+      c.y = unorm8(r.color.y);
+      c.z = unorm8(r.color.z);
+    } else {
+      c.x = c.y = c.z = 0;
+    }
+    c.w = 255;
+    f.color[idx] = c;
+  }
+  if (f.mapping) f.mapping[idx] = make_float4(r.p.x, r.p.y, r.p.z, 1.0f);
+  if (f.hit) f.hit[idx] = r.has_color ? r.face : -1;
+  if (f.steps) f.steps[idx] = r.steps;
+}
+
+// --------------------------------------------------------------------------
+// Shared-memory staging of small scenes with one TMA bulk copy
+// (cp.async.bulk global -> shared, completion on an mbarrier).  The wait is
+// bounded: after the budget the kernel flags LINON error bit 1, waits once
+// more (bounded) for its own copy, and falls back to global memory.
+// --------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned phase) {
+  unsigned done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(bar), "r"(phase)
+      : "memory");
+  return done != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned phase, int budget) {
+  for (int i = 0; i < budget; ++i)
+    if (mbar_try_wait(bar, phase)) return true;
+  return false;
+}
+
+// Copies `bytes` (multiple of 16, both pointers 16-byte aligned) into smem.
+// All threads of the CTA call it; returns true when the copy is usable.
+__device__ __forceinline__ bool stage_to_smem(void* smem, const void* gmem, unsigned bytes,
+                                              unsigned long long* mbar, int* err) {
+  const unsigned bar = smem_addr(mbar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(1) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(smem)),
+        "l"(gmem), "r"(bytes), "r"(bar)
+        : "memory");
+  }
+  bool ok = mbar_wait_bounded(bar, 0, 1 << 20);
+  if (!ok) {
+    atomicOr(err, 1);
+    ok = mbar_wait_bounded(bar, 0, 1 << 22);
+  }
+  // every thread must agree before the smem copy is used
+  ok = __syncthreads_and(ok ? 1 : 0) != 0;
+  return ok;
+}
+
+// Sets up the scene view of a CTA: small scenes come from shared memory.
+__device__ __forceinline__ SceneView cta_scene(const DevScene& s, float4* smem,
+                                               unsigned long long* mbar, int* err) {
+  SceneView v;
+  v.tris = s.tris;
+  v.nodes = s.nodes;
+  v.face_rgb = s.face_rgb;
+  v.n_tris = s.n_tris;
+  v.n_nodes = s.n_nodes;
+  if (s.staged_bytes > 0) {
+    // staged block = [nodes | tris] contiguous in global memory
+    if (stage_to_smem(smem, s.staged, (unsigned)s.staged_bytes, mbar, err)) {
+      v.nodes = smem;
+      v.tris = smem + 2 * s.n_nodes;
+    }
+  }
+  return v;
+}
+
+// --------------------------------------------------------------------------
+// Kernels (instantiated per field by the generated module)
+// --------------------------------------------------------------------------
+
+// One thread per pixel; the CTA covers a tile_w x tile_h pixel tile.
+template <bool ADAPTIVE, bool KAHAN, class F>
+__device__ __forceinline__ void march_plain_kernel(const F& field, const MarchArgs& a) {
+  extern __shared__ float4 linon_smem[];
+  __shared__ unsigned long long mbar;
+  const SceneView sc = cta_scene(a.scene, linon_smem, &mbar, a.err);
+  const int W = a.frame.W, H = a.frame.H;
+  const int lx = threadIdx.x % a.tile_w, ly = threadIdx.x / a.tile_w;
+  const int x = blockIdx.x * a.tile_w + lx;
+  const int row = blockIdx.y * a.tile_h + ly;
+  if (x >= W || row >= H) return;
+  const int gy = H - 1 - row;
+  const Basis b = make_basis(a.cam, W, H, a.m.focal_length, a.m.viewport_height);
+  const vec3f dir = primary_dir(b, x, gy);
+  const size_t idx = size_t(row) * W + x;
+  RayState r;
+  ray_init(r, b.origin, dir, a.m.h_initial);
+  if (a.m.linear_mode) {  // main_view.wgsl:368-370
+    HitRec hit = intersect_segment(sc, b.origin, dir, 100.0f, b.origin + 100.0f * dir, a.err);
+    wgsl::vec4f c(0.0f, 0.0f, 0.0f, 0.0f);
+    if (hit.t > 0.0f && hit.t < 100.0f) c = shade_hit(sc, hit, dir);
+    if (a.frame.color) {
+      uchar4 o;
+      o.x = unorm8(c.x); o.y = unorm8(c.y); o.z = unorm8(c.z); o.w = unorm8(c.w);
+      a.frame.color[idx] = o;
+    }
+    if (a.frame.hit) a.frame.hit[idx] = hit.t > 0.0f && hit.t < 100.0f ? hit.id : -1;
+    if (a.frame.mapping) a.frame.mapping[idx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (a.frame.steps) a.frame.steps[idx] = 0;
+    return;
+  }
+  while (ray_active(r, a.m)) ray_step<ADAPTIVE, KAHAN>(r, field, a.m, sc, a.err);
+  ray_store(r, a.frame, idx);
+}
+
+// --------------------------------------------------------------------------
+// Persistent batched march: many views of uneven size, camera, step size and
+// field in one launch.  Work comes from a device queue: a 64-bit counter over
+// the concatenated ray space of all views (each view's rays ordered in
+// tile_w x tile_h pixel tiles of 32 rays, so consecutive rays are image
+// neighbours).  Each warp owns 32 ray slots; every `quantum` RK4 steps it
+// retires finished rays (storing their pixels) and refills the free slots with
+// one atomicAdd on the counter (persistent "while-while" ray scheduling,
+// Aila & Laine 2009).  Warps exit when the queue is drained and their slots
+// are empty.
+// --------------------------------------------------------------------------
+template <class F>
+__device__ __forceinline__ void ray_step_rt(RayState& r, const F& field, const DevMarch& m,
+                                            const SceneView& sc, int* err) {
+  if (m.adaptive) {
+    if (m.kahan) ray_step<true, true>(r, field, m, sc, err);
+    else ray_step<true, false>(r, field, m, sc, err);
+  } else {
+    if (m.kahan) ray_step<false, true>(r, field, m, sc, err);
+    else ray_step<false, false>(r, field, m, sc, err);
+  }
+}
+
+template <class Fields>
+struct FieldRef {
+  const Fields& f;
+  int i;
+  __device__ __forceinline__ vec3f operator()(const vec3f& pp, const vec3f& p, const vec3f& v0,
+                                              const vec3f& v, float t) const {
+    return f(i, pp, p, v0, v, t);
+  }
+};
+
+__device__ __forceinline__ int find_view(const BatchArgs& a, long long gid) {
+  int lo = 0, hi = a.n_views - 1;  // last view with ray_begin <= gid
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (a.views[mid].ray_begin <= gid) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <class Fields>
+__device__ __forceinline__ void march_batch_kernel(const Fields& fields, const BatchArgs& a) {
+  extern __shared__ float4 linon_smem[];
+  __shared__ unsigned long long mbar;
+  const SceneView sc = cta_scene(a.scene, linon_smem, &mbar, a.err);
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  RayState r;
+  DevMarch m;
+  DevFrame out;
+  size_t pix = 0;
+  int fidx = 0;
+  bool active = false;
+  bool drained = false;
+  for (;;) {
+    // ---- refill free slots from the queue ----
+    if (!drained) {
+      const unsigned free_mask = __ballot_sync(FULL, !active);
+      if (free_mask) {
+        const int nfree = __popc(free_mask);
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(a.counter, (unsigned long long)nfree);
+        base = __shfl_sync(FULL, base, 0);
+        if (base + nfree >= (unsigned long long)a.total_rays) drained = true;
+        if (!active) {
+          const long long gid = (long long)base + __popc(free_mask & ((1u << lane) - 1));
+          if (gid < a.total_rays) {
+            const int view = find_view(a, gid);
+            const BatchView& V = a.views[view];
+            const long long local = gid - V.ray_begin;
+            const int tile = int(local / (a.tile_w * a.tile_h));
+            const int within = int(local % (a.tile_w * a.tile_h));
+            const int x = (tile % V.tiles_x) * a.tile_w + within % a.tile_w;
+            const int row = (tile / V.tiles_x) * a.tile_h + within / a.tile_w;
+            if (x < V.frame.W && row < V.frame.H) {
+              m = V.m;
+              out = V.frame;
+              fidx = V.field;
+              pix = size_t(row) * V.frame.W + x;
+              const Basis b = make_basis(V.cam, V.frame.W, V.frame.H, m.focal_length, m.viewport_height);
+              const vec3f dir = primary_dir(b, x, V.frame.H - 1 - row);
+              ray_init(r, b.origin, dir, m.h_initial);
+              active = true;
+              if (m.linear_mode) {
+                HitRec hit = intersect_segment(sc, b.origin, dir, 100.0f, b.origin + 100.0f * dir, a.err);
+                wgsl::vec4f c(0.0f, 0.0f, 0.0f, 0.0f);
+                if (hit.t > 0.0f && hit.t < 100.0f) c = shade_hit(sc, hit, dir);
+                if (out.color) {
+                  uchar4 o;
+                  o.x = unorm8(c.x); o.y = unorm8(c.y); o.z = unorm8(c.z); o.w = unorm8(c.w);
+                  out.color[pix] = o;
+                }
+                if (out.hit) out.hit[pix] = hit.t > 0.0f && hit.t < 100.0f ? hit.id : -1;
+                if (out.mapping) out.mapping[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                if (out.steps) out.steps[pix] = 0;
+                active = false;
+              }
+            }
+          }
+        }
+      }
+    }
+    if (!__any_sync(FULL, active)) {
+      if (drained) break;
+      continue;
+    }
+    // ---- march a quantum ----
+    if (active) {
+      const FieldRef<Fields> field{fields, fidx};
+      for (int q = 0; q < a.quantum; ++q) {
+        if (!ray_active(r, m)) break;
+        ray_step_rt(r, field, m, sc, a.err);
+      }
+      if (!ray_active(r, m)) {
+        ray_store(r, out, pix);
+        active = false;
+      }
+    }
+  }
+}
+
+// sample_rays generalised: one thread per ray; out[ray][point] float4.
+template <class F>
+__device__ __forceinline__ void capture_kernel(const F& field, const CaptureArgs& a) {
+  const int ray = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ray >= a.n_rays) return;
+  const Basis b = make_basis(a.cam, a.W, a.H, a.focal_length, a.viewport_height);
+  const vec3f start_dir = position_dir(b, a.pos[2 * ray], a.pos[2 * ray + 1]);
+  vec3f p = b.origin, dir = start_dir;
+  float t = 0.0f;
+  const float h = a.h, hh = 0.5f * a.h, w = a.field_weight;
+  float4* out = a.out + size_t(ray) * a.n_points;
+  for (int i = 0; i < a.n_steps; ++i) {
+    const vec3f k1 = field(p, p, start_dir, dir, t);
+    const vec3f k2 = field(p, p + hh * k1, start_dir, k1, t + hh);
+    const vec3f k3 = field(p, p + hh * k2, start_dir, k2, t + hh);
+    const vec3f k4 = field(p, p + h * k3, start_dir, k3, t + h);
+    const vec3f v = LINON_DIV6(((k1 + 2.0f * k2) + 2.0f * k3) + k4);
+    dir = (1.0f - w) * dir + w * v;
+    const vec3f step_dir = dir * h;
+    if (i % a.every == 0) out[i / a.every] = make_float4(p.x, p.y, p.z, 1.0f);
+    p = p + step_dir;
+    t = t + h;
+  }
+  if (a.record_final) out[a.n_points - 1] = make_float4(p.x, p.y, p.z, 1.0f);
+}
+
+// Field evaluation at listed inputs (13 floats each) for front-end tests.
+template <class F>
+__device__ __forceinline__ void field_eval_kernel(const F& field, const float* in, float* out,
+                                                  int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* q = in + 13 * size_t(i);
+  vec3f r = field(vec3f(q[0], q[1], q[2]), vec3f(q[3], q[4], q[5]), vec3f(q[6], q[7], q[8]),
+                  vec3f(q[9], q[10], q[11]), q[12]);
+  out[3 * size_t(i)] = r.x;
+  out[3 * size_t(i) + 1] = r.y;
+  out[3 * size_t(i) + 2] = r.z;
+}
+
+}  // namespace linon

@@ -1,0 +1,498 @@
+// wgsl_rt.cuh — the WGSL value types, builtins and linon helper functions
+// that field functions lowered by the WGSL front end are written against.
+//
+// Compiled three ways: by NVRTC into every march module (device), by nvcc into
+// the ahead-of-time kernels, and by a host C++ compiler when the test suite
+// checks the front end's output on the CPU.  No system headers are needed on
+// the device side (NVRTC provides the CUDA math functions).
+//
+// Semantics follow the WGSL spec; where WGSL leaves a choice to the
+// implementation this file makes the same choice as the FP32 restatement of
+// the shader (dot sums x,y then z; M*v sums columns in order; clamp(e,lo,hi)
+// = min(max(e,lo),hi); min/max are IEEE fmin/fmax).  With LINON_PRECISE
+// defined every builtin is op-for-op that restatement; otherwise normalize and
+// inverseSqrt use the hardware reciprocal square root.
+#pragma once
+
+#if defined(__CUDACC__)
+#define WG_HD __host__ __device__ __forceinline__
+#else
+#define WG_HD inline
+#include <math.h>
+#endif
+
+namespace wgsl {
+
+// ---------------------------------------------------------------------------
+// scalar math
+// ---------------------------------------------------------------------------
+WG_HD float rsqrt_(float x) {
+#if defined(__CUDA_ARCH__) && !defined(LINON_PRECISE)
+  return rsqrtf(x);
+#else
+  return 1.0f / sqrtf(x);
+#endif
+}
+WG_HD float fmin_(float a, float b) { return fminf(a, b); }
+WG_HD float fmax_(float a, float b) { return fmaxf(a, b); }
+WG_HD int imin_(int a, int b) { return a < b ? a : b; }
+WG_HD int imax_(int a, int b) { return a > b ? a : b; }
+WG_HD unsigned umin_(unsigned a, unsigned b) { return a < b ? a : b; }
+WG_HD unsigned umax_(unsigned a, unsigned b) { return a > b ? a : b; }
+WG_HD float f32_from_bits(unsigned u) {
+  union { unsigned u; float f; } c;
+  c.u = u;
+  return c.f;
+}
+// f32 -> i32 / u32 conversions saturate (WGSL conversion rules); NaN -> 0
+WG_HD int to_i32(float x) {
+  if (!(x == x)) return 0;
+  if (x >= 2147483520.0f) return 2147483647;
+  if (x <= -2147483648.0f) return -2147483647 - 1;
+  return int(x);
+}
+WG_HD int to_i32(int x) { return x; }
+WG_HD int to_i32(unsigned x) { return int(x); }
+WG_HD unsigned to_u32(float x) {
+  if (!(x == x) || x <= 0.0f) return 0u;
+  if (x >= 4294967040.0f) return 4294967295u;
+  return unsigned(x);
+}
+WG_HD unsigned to_u32(int x) { return unsigned(x); }
+WG_HD unsigned to_u32(unsigned x) { return x; }
+
+// ---------------------------------------------------------------------------
+// vectors
+// ---------------------------------------------------------------------------
+template <class T, int N> struct vec;
+
+template <class T> struct vec<T, 2> {
+  T x, y;
+  WG_HD vec() : x(T(0)), y(T(0)) {}
+  WG_HD vec(T a, T b) : x(a), y(b) {}
+  WG_HD explicit vec(T s) : x(s), y(s) {}
+  template <class U> WG_HD explicit vec(const vec<U, 2>& o) : x(T(o.x)), y(T(o.y)) {}
+  WG_HD T& operator[](int i) { return i == 0 ? x : y; }
+  WG_HD T operator[](int i) const { return i == 0 ? x : y; }
+};
+template <class T> struct vec<T, 3> {
+  T x, y, z;
+  WG_HD vec() : x(T(0)), y(T(0)), z(T(0)) {}
+  WG_HD vec(T a, T b, T c) : x(a), y(b), z(c) {}
+  WG_HD explicit vec(T s) : x(s), y(s), z(s) {}
+  WG_HD vec(const vec<T, 2>& a, T c) : x(a.x), y(a.y), z(c) {}
+  WG_HD vec(T a, const vec<T, 2>& b) : x(a), y(b.x), z(b.y) {}
+  template <class U> WG_HD explicit vec(const vec<U, 3>& o) : x(T(o.x)), y(T(o.y)), z(T(o.z)) {}
+  WG_HD T& operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+  WG_HD T operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+template <class T> struct vec<T, 4> {
+  T x, y, z, w;
+  WG_HD vec() : x(T(0)), y(T(0)), z(T(0)), w(T(0)) {}
+  WG_HD vec(T a, T b, T c, T d) : x(a), y(b), z(c), w(d) {}
+  WG_HD explicit vec(T s) : x(s), y(s), z(s), w(s) {}
+  WG_HD vec(const vec<T, 3>& a, T d) : x(a.x), y(a.y), z(a.z), w(d) {}
+  WG_HD vec(T a, const vec<T, 3>& b) : x(a), y(b.x), z(b.y), w(b.z) {}
+  WG_HD vec(const vec<T, 2>& a, const vec<T, 2>& b) : x(a.x), y(a.y), z(b.x), w(b.y) {}
+  WG_HD vec(const vec<T, 2>& a, T c, T d) : x(a.x), y(a.y), z(c), w(d) {}
+  WG_HD vec(T a, const vec<T, 2>& b, T d) : x(a), y(b.x), z(b.y), w(d) {}
+  WG_HD vec(T a, T b, const vec<T, 2>& c) : x(a), y(b), z(c.x), w(c.y) {}
+  template <class U>
+  WG_HD explicit vec(const vec<U, 4>& o) : x(T(o.x)), y(T(o.y)), z(T(o.z)), w(T(o.w)) {}
+  WG_HD T& operator[](int i) { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
+  WG_HD T operator[](int i) const { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
+};
+
+typedef vec<float, 2> vec2f;
+typedef vec<float, 3> vec3f;
+typedef vec<float, 4> vec4f;
+typedef vec<int, 2> vec2i;
+typedef vec<int, 3> vec3i;
+typedef vec<int, 4> vec4i;
+typedef vec<unsigned, 2> vec2u;
+typedef vec<unsigned, 3> vec3u;
+typedef vec<unsigned, 4> vec4u;
+typedef vec<bool, 2> vec2b;
+typedef vec<bool, 3> vec3b;
+typedef vec<bool, 4> vec4b;
+
+// swizzle: swz<i,j,...>(v) evaluates v once.
+template <int A, int B, class T, int N> WG_HD vec<T, 2> swz(const vec<T, N>& v) {
+  return vec<T, 2>(v[A], v[B]);
+}
+template <int A, int B, int C, class T, int N> WG_HD vec<T, 3> swz(const vec<T, N>& v) {
+  return vec<T, 3>(v[A], v[B], v[C]);
+}
+template <int A, int B, int C, int D, class T, int N> WG_HD vec<T, 4> swz(const vec<T, N>& v) {
+  return vec<T, 4>(v[A], v[B], v[C], v[D]);
+}
+
+#define WG_VEC_BINOP(OP)                                                         \
+  template <class T, int N> WG_HD vec<T, N> operator OP(const vec<T, N>& a,     \
+                                                         const vec<T, N>& b) {  \
+    vec<T, N> r;                                                                 \
+    for (int i = 0; i < N; ++i) r[i] = a[i] OP b[i];                             \
+    return r;                                                                    \
+  }                                                                              \
+  template <class T, int N> WG_HD vec<T, N> operator OP(const vec<T, N>& a, T s) { \
+    vec<T, N> r;                                                                 \
+    for (int i = 0; i < N; ++i) r[i] = a[i] OP s;                                \
+    return r;                                                                    \
+  }                                                                              \
+  template <class T, int N> WG_HD vec<T, N> operator OP(T s, const vec<T, N>& a) { \
+    vec<T, N> r;                                                                 \
+    for (int i = 0; i < N; ++i) r[i] = s OP a[i];                                \
+    return r;                                                                    \
+  }
+WG_VEC_BINOP(+)
+WG_VEC_BINOP(-)
+WG_VEC_BINOP(*)
+WG_VEC_BINOP(/)
+#undef WG_VEC_BINOP
+
+template <class T, int N> WG_HD vec<T, N> operator-(const vec<T, N>& a) {
+  vec<T, N> r;
+  for (int i = 0; i < N; ++i) r[i] = -a[i];
+  return r;
+}
+template <int N> WG_HD vec<bool, N> operator!(const vec<bool, N>& a) {
+  vec<bool, N> r;
+  for (int i = 0; i < N; ++i) r[i] = !a[i];
+  return r;
+}
+template <class T, int N> WG_HD vec<T, N>& operator+=(vec<T, N>& a, const vec<T, N>& b) { a = a + b; return a; }
+template <class T, int N> WG_HD vec<T, N>& operator-=(vec<T, N>& a, const vec<T, N>& b) { a = a - b; return a; }
+template <class T, int N> WG_HD vec<T, N>& operator*=(vec<T, N>& a, const vec<T, N>& b) { a = a * b; return a; }
+template <class T, int N> WG_HD vec<T, N>& operator/=(vec<T, N>& a, const vec<T, N>& b) { a = a / b; return a; }
+template <class T, int N> WG_HD vec<T, N>& operator+=(vec<T, N>& a, T b) { a = a + b; return a; }
+template <class T, int N> WG_HD vec<T, N>& operator-=(vec<T, N>& a, T b) { a = a - b; return a; }
+template <class T, int N> WG_HD vec<T, N>& operator*=(vec<T, N>& a, T b) { a = a * b; return a; }
+template <class T, int N> WG_HD vec<T, N>& operator/=(vec<T, N>& a, T b) { a = a / b; return a; }
+
+// component-wise comparisons (vector results)
+#define WG_VEC_CMP(NAME, OP)                                                            \
+  template <class T, int N> WG_HD vec<bool, N> NAME(const vec<T, N>& a, const vec<T, N>& b) { \
+    vec<bool, N> r;                                                                     \
+    for (int i = 0; i < N; ++i) r[i] = a[i] OP b[i];                                    \
+    return r;                                                                           \
+  }                                                                                     \
+  template <class T> WG_HD bool NAME(T a, T b) { return a OP b; }
+WG_VEC_CMP(cmp_lt, <)
+WG_VEC_CMP(cmp_le, <=)
+WG_VEC_CMP(cmp_gt, >)
+WG_VEC_CMP(cmp_ge, >=)
+WG_VEC_CMP(cmp_eq, ==)
+WG_VEC_CMP(cmp_ne, !=)
+#undef WG_VEC_CMP
+template <int N> WG_HD vec<bool, N> land(const vec<bool, N>& a, const vec<bool, N>& b) {
+  vec<bool, N> r;
+  for (int i = 0; i < N; ++i) r[i] = a[i] && b[i];
+  return r;
+}
+template <int N> WG_HD vec<bool, N> lor(const vec<bool, N>& a, const vec<bool, N>& b) {
+  vec<bool, N> r;
+  for (int i = 0; i < N; ++i) r[i] = a[i] || b[i];
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// matrices (column major, C columns of R rows)
+// ---------------------------------------------------------------------------
+template <int C, int R> struct mat {
+  vec<float, R> c[C];
+  WG_HD mat() {}
+  WG_HD vec<float, R>& operator[](int i) { return c[i]; }
+  WG_HD const vec<float, R>& operator[](int i) const { return c[i]; }
+};
+template <int R> WG_HD mat<2, R> make_mat(const vec<float, R>& a, const vec<float, R>& b) {
+  mat<2, R> m; m.c[0] = a; m.c[1] = b; return m;
+}
+template <int R>
+WG_HD mat<3, R> make_mat(const vec<float, R>& a, const vec<float, R>& b, const vec<float, R>& c) {
+  mat<3, R> m; m.c[0] = a; m.c[1] = b; m.c[2] = c; return m;
+}
+template <int R>
+WG_HD mat<4, R> make_mat(const vec<float, R>& a, const vec<float, R>& b, const vec<float, R>& c,
+                         const vec<float, R>& d) {
+  mat<4, R> m; m.c[0] = a; m.c[1] = b; m.c[2] = c; m.c[3] = d; return m;
+}
+// matrix * vector: columns summed in order
+template <int C, int R> WG_HD vec<float, R> operator*(const mat<C, R>& m, const vec<float, C>& v) {
+  vec<float, R> r = m.c[0] * v[0];
+  for (int k = 1; k < C; ++k) r = r + m.c[k] * v[k];
+  return r;
+}
+template <int C, int R> WG_HD vec<float, C> operator*(const vec<float, R>& v, const mat<C, R>& m) {
+  vec<float, C> r;
+  for (int i = 0; i < C; ++i) {
+    float s = v[0] * m.c[i][0];
+    for (int k = 1; k < R; ++k) s = s + v[k] * m.c[i][k];
+    r[i] = s;
+  }
+  return r;
+}
+template <int K, int R, int C2> WG_HD mat<C2, R> operator*(const mat<K, R>& a, const mat<C2, K>& b) {
+  mat<C2, R> m;
+  for (int j = 0; j < C2; ++j) m.c[j] = a * b.c[j];
+  return m;
+}
+template <int C, int R> WG_HD mat<C, R> operator*(const mat<C, R>& a, float s) {
+  mat<C, R> m;
+  for (int j = 0; j < C; ++j) m.c[j] = a.c[j] * s;
+  return m;
+}
+template <int C, int R> WG_HD mat<C, R> operator*(float s, const mat<C, R>& a) {
+  mat<C, R> m;
+  for (int j = 0; j < C; ++j) m.c[j] = s * a.c[j];
+  return m;
+}
+template <int C, int R> WG_HD mat<C, R> operator+(const mat<C, R>& a, const mat<C, R>& b) {
+  mat<C, R> m;
+  for (int j = 0; j < C; ++j) m.c[j] = a.c[j] + b.c[j];
+  return m;
+}
+template <int C, int R> WG_HD mat<C, R> operator-(const mat<C, R>& a, const mat<C, R>& b) {
+  mat<C, R> m;
+  for (int j = 0; j < C; ++j) m.c[j] = a.c[j] - b.c[j];
+  return m;
+}
+template <int C, int R> WG_HD mat<C, R> operator-(const mat<C, R>& a) {
+  mat<C, R> m;
+  for (int j = 0; j < C; ++j) m.c[j] = -a.c[j];
+  return m;
+}
+template <int C, int R> WG_HD mat<R, C> transpose(const mat<C, R>& a) {
+  mat<R, C> m;
+  for (int j = 0; j < C; ++j)
+    for (int i = 0; i < R; ++i) m.c[i][j] = a.c[j][i];
+  return m;
+}
+WG_HD float determinant(const mat<2, 2>& m) { return m.c[0].x * m.c[1].y - m.c[1].x * m.c[0].y; }
+WG_HD float determinant(const mat<3, 3>& m) {
+  return m.c[0].x * (m.c[1].y * m.c[2].z - m.c[2].y * m.c[1].z) -
+         m.c[1].x * (m.c[0].y * m.c[2].z - m.c[2].y * m.c[0].z) +
+         m.c[2].x * (m.c[0].y * m.c[1].z - m.c[1].y * m.c[0].z);
+}
+
+// ---------------------------------------------------------------------------
+// builtins
+// ---------------------------------------------------------------------------
+#define WG_UNARY(NAME, EXPR)                                                       \
+  WG_HD float NAME(float x) { return EXPR; }                                       \
+  template <int N> WG_HD vec<float, N> NAME(const vec<float, N>& v) {              \
+    vec<float, N> r;                                                               \
+    for (int i = 0; i < N; ++i) r[i] = NAME(v[i]);                                 \
+    return r;                                                                      \
+  }
+WG_UNARY(sin, sinf(x))
+WG_UNARY(cos, cosf(x))
+WG_UNARY(tan, tanf(x))
+WG_UNARY(asin, asinf(x))
+WG_UNARY(acos, acosf(x))
+WG_UNARY(atan, atanf(x))
+WG_UNARY(sinh, sinhf(x))
+WG_UNARY(cosh, coshf(x))
+WG_UNARY(tanh, tanhf(x))
+WG_UNARY(asinh, asinhf(x))
+WG_UNARY(acosh, acoshf(x))
+WG_UNARY(atanh, atanhf(x))
+WG_UNARY(exp, expf(x))
+WG_UNARY(exp2, exp2f(x))
+WG_UNARY(log, logf(x))
+WG_UNARY(log2, log2f(x))
+WG_UNARY(sqrt, sqrtf(x))
+WG_UNARY(inverseSqrt, rsqrt_(x))
+WG_UNARY(floor, floorf(x))
+WG_UNARY(ceil, ceilf(x))
+WG_UNARY(trunc, truncf(x))
+WG_UNARY(round, rintf(x))
+WG_UNARY(fract, x - floorf(x))
+WG_UNARY(sign, (x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f)))
+WG_UNARY(saturate, fmin_(fmax_(x, 0.0f), 1.0f))
+WG_UNARY(degrees, x * 57.295779513082323f)
+WG_UNARY(radians, x * 0.017453292519943295f)
+#undef WG_UNARY
+
+WG_HD float abs(float x) { return fabsf(x); }
+WG_HD int abs(int x) { return x < 0 ? -x : x; }
+WG_HD unsigned abs(unsigned x) { return x; }
+template <class T, int N> WG_HD vec<T, N> abs(const vec<T, N>& v) {
+  vec<T, N> r;
+  for (int i = 0; i < N; ++i) r[i] = abs(v[i]);
+  return r;
+}
+
+#define WG_BINARY(NAME, EXPR)                                                          \
+  WG_HD float NAME(float a, float b) { return EXPR; }                                  \
+  template <int N> WG_HD vec<float, N> NAME(const vec<float, N>& a, const vec<float, N>& b) { \
+    vec<float, N> r;                                                                   \
+    for (int i = 0; i < N; ++i) r[i] = NAME(a[i], b[i]);                               \
+    return r;                                                                          \
+  }
+WG_BINARY(pow, powf(a, b))
+WG_BINARY(atan2, atan2f(a, b))
+WG_BINARY(step, (b >= a ? 1.0f : 0.0f))
+WG_BINARY(fmod_wgsl, (a - b * truncf(a / b)))
+#undef WG_BINARY
+
+WG_HD float min(float a, float b) { return fmin_(a, b); }
+WG_HD float max(float a, float b) { return fmax_(a, b); }
+WG_HD int min(int a, int b) { return imin_(a, b); }
+WG_HD int max(int a, int b) { return imax_(a, b); }
+WG_HD unsigned min(unsigned a, unsigned b) { return umin_(a, b); }
+WG_HD unsigned max(unsigned a, unsigned b) { return umax_(a, b); }
+template <class T, int N> WG_HD vec<T, N> min(const vec<T, N>& a, const vec<T, N>& b) {
+  vec<T, N> r;
+  for (int i = 0; i < N; ++i) r[i] = min(a[i], b[i]);
+  return r;
+}
+template <class T, int N> WG_HD vec<T, N> max(const vec<T, N>& a, const vec<T, N>& b) {
+  vec<T, N> r;
+  for (int i = 0; i < N; ++i) r[i] = max(a[i], b[i]);
+  return r;
+}
+template <class T> WG_HD T clamp(T e, T lo, T hi) { return min(max(e, lo), hi); }
+template <class T, int N>
+WG_HD vec<T, N> clamp(const vec<T, N>& e, const vec<T, N>& lo, const vec<T, N>& hi) {
+  return min(max(e, lo), hi);
+}
+WG_HD float fma(float a, float b, float c) { return fmaf(a, b, c); }
+template <int N>
+WG_HD vec<float, N> fma(const vec<float, N>& a, const vec<float, N>& b, const vec<float, N>& c) {
+  vec<float, N> r;
+  for (int i = 0; i < N; ++i) r[i] = fmaf(a[i], b[i], c[i]);
+  return r;
+}
+// mix(e1, e2, e3) = e1 * (1 - e3) + e2 * e3
+WG_HD float mix(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+template <int N> WG_HD vec<float, N> mix(const vec<float, N>& a, const vec<float, N>& b, float t) {
+  return a * (1.0f - t) + b * t;
+}
+template <int N>
+WG_HD vec<float, N> mix(const vec<float, N>& a, const vec<float, N>& b, const vec<float, N>& t) {
+  return a * (vec<float, N>(1.0f) - t) + b * t;
+}
+WG_HD float smoothstep(float lo, float hi, float x) {
+  float t = clamp((x - lo) / (hi - lo), 0.0f, 1.0f);
+  return t * t * (3.0f - 2.0f * t);
+}
+template <int N>
+WG_HD vec<float, N> smoothstep(const vec<float, N>& lo, const vec<float, N>& hi,
+                               const vec<float, N>& x) {
+  vec<float, N> r;
+  for (int i = 0; i < N; ++i) r[i] = smoothstep(lo[i], hi[i], x[i]);
+  return r;
+}
+
+WG_HD float dot(const vec2f& a, const vec2f& b) { return a.x * b.x + a.y * b.y; }
+WG_HD float dot(const vec3f& a, const vec3f& b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+WG_HD float dot(const vec4f& a, const vec4f& b) {
+  return ((a.x * b.x + a.y * b.y) + a.z * b.z) + a.w * b.w;
+}
+WG_HD int dot(const vec2i& a, const vec2i& b) { return a.x * b.x + a.y * b.y; }
+WG_HD int dot(const vec3i& a, const vec3i& b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+WG_HD vec3f cross(const vec3f& a, const vec3f& b) {
+  return vec3f(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+WG_HD float length(float x) { return fabsf(x); }
+template <int N> WG_HD float length(const vec<float, N>& v) { return sqrtf(dot(v, v)); }
+template <int N> WG_HD float distance(const vec<float, N>& a, const vec<float, N>& b) {
+  return length(a - b);
+}
+WG_HD float distance(float a, float b) { return fabsf(a - b); }
+template <int N> WG_HD vec<float, N> normalize(const vec<float, N>& v) {
+#if defined(LINON_PRECISE) || !defined(__CUDA_ARCH__)
+  float l = sqrtf(dot(v, v));
+  return v / l;
+#else
+  return v * rsqrtf(dot(v, v));
+#endif
+}
+// reflect(e1, e2) = e1 - 2 * dot(e2, e1) * e2
+template <int N> WG_HD vec<float, N> reflect(const vec<float, N>& e1, const vec<float, N>& e2) {
+  float d = 2.0f * dot(e2, e1);
+  return e1 - d * e2;
+}
+template <int N>
+WG_HD vec<float, N> refract(const vec<float, N>& e1, const vec<float, N>& e2, float e3) {
+  float d = dot(e2, e1);
+  float k = 1.0f - e3 * e3 * (1.0f - d * d);
+  if (k < 0.0f) return vec<float, N>(0.0f);
+  return e3 * e1 - (e3 * d + sqrtf(k)) * e2;
+}
+template <int N>
+WG_HD vec<float, N> faceForward(const vec<float, N>& e1, const vec<float, N>& e2,
+                                const vec<float, N>& e3) {
+  return dot(e2, e3) < 0.0f ? e1 : -e1;
+}
+// select(f, t, cond)
+template <class T> WG_HD T select(const T& f, const T& t, bool c) { return c ? t : f; }
+template <class T, int N>
+WG_HD vec<T, N> select(const vec<T, N>& f, const vec<T, N>& t, const vec<bool, N>& c) {
+  vec<T, N> r;
+  for (int i = 0; i < N; ++i) r[i] = c[i] ? t[i] : f[i];
+  return r;
+}
+WG_HD bool all(bool b) { return b; }
+WG_HD bool any(bool b) { return b; }
+template <int N> WG_HD bool all(const vec<bool, N>& v) {
+  bool r = true;
+  for (int i = 0; i < N; ++i) r = r && v[i];
+  return r;
+}
+template <int N> WG_HD bool any(const vec<bool, N>& v) {
+  bool r = false;
+  for (int i = 0; i < N; ++i) r = r || v[i];
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// linon helper functions, src/main_view.wgsl:76-146
+// ---------------------------------------------------------------------------
+#define LINON_PI 3.14159265358979323846f
+
+WG_HD vec3f rotateX(const vec3f& v, float phi) {  // main_view.wgsl:78-84
+  float c = cosf(phi), s = sinf(phi);
+  return make_mat(vec3f(1.0f, 0.0f, 0.0f), vec3f(0.0f, c, s), vec3f(0.0f, -s, c)) * v;
+}
+WG_HD vec3f rotateY(const vec3f& v, float phi) {  // main_view.wgsl:86-92
+  float c = cosf(phi), s = sinf(phi);
+  return make_mat(vec3f(c, 0.0f, -s), vec3f(0.0f, 1.0f, 0.0f), vec3f(s, 0.0f, c)) * v;
+}
+WG_HD vec3f rotateZ(const vec3f& v, float phi) {  // main_view.wgsl:94-100: third column zero
+  float c = cosf(phi), s = sinf(phi);
+  return make_mat(vec3f(c, s, 0.0f), vec3f(-s, c, 0.0f), vec3f(0.0f, 0.0f, 0.0f)) * v;
+}
+WG_HD vec3f translate(const vec3f& v, float dx, float dy, float dz) {  // main_view.wgsl:102-108
+  return vec3f(v.x + dx, v.y + dy, v.z + dz);
+}
+WG_HD float refraction_index(float t) {  // main_view.wgsl:111-117 (Y. Zhao et al.)
+  const float air_pressure = 101325.0f;
+  const float c1 = 0.0000104f;
+  const float c2 = 0.00366f;
+  return c1 * air_pressure * (1.0f + air_pressure * (60.1f - 0.972f * t) * 1e-10f) /
+         (1.0f + c2 * t);
+}
+WG_HD vec3f refraction(float t_in, float t_out, const vec3f& v_in, const vec3f& n) {
+  // main_view.wgsl:119-136; clamp(-1.0, 1.0, x) == min(1, x)
+  float eta_in = refraction_index(t_in);
+  float eta_out = refraction_index(t_out);
+  float cosi = clamp(-1.0f, 1.0f, dot(v_in, n));
+  vec3f n_ref = n;
+  if (cosi < 0.0f) {
+    cosi = -cosi;
+  } else {
+    n_ref = -n;
+  }
+  float eta = eta_in / eta_out;
+  float k = 1.0f - eta * eta * (1.0f - cosi * cosi);
+  if (k < 0.0f) return reflect(v_in, n_ref);
+  return eta * v_in + (eta * cosi - sqrtf(k)) * n_ref;
+}
+WG_HD float point_plane_distance(const vec3f& p, const vec3f& n, const vec3f& p0) {
+  float d = dot(p0, n);  // main_view.wgsl:138-142
+  return fabsf(dot(p, n) - d);
+}
+WG_HD float sigmoid(float x) { return 1.0f / (1.0f + expf(-x)); }  // main_view.wgsl:144-146
+
+}  // namespace wgsl

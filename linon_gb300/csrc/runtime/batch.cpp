@@ -1,0 +1,336 @@
+// batch.cpp — batched rendering of many views in one persistent launch.
+//
+// The reference renders one view per dispatch (MainView::render,
+// src/main_view.rs:831-849) and re-renders at h = 0.001 for Enhance
+// (src/main_view.rs:778-802).  Here any number of views (different size,
+// camera, step size and field) go into one persistent kernel fed by a device
+// work queue; the launch (queue reset + kernel) is captured in a CUDA graph
+// and replayed while the batch shape stays the same.  An autotuner sweeps
+// quantum x block size x tile shape on the caller's batch and caches the
+// winner in the context.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <sstream>
+
+#include "internal.hpp"
+
+namespace linon {
+namespace {
+
+struct BatchState {
+  DevBuf views;    // BatchView table
+  DevBuf counter;  // queue head
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<char> key;  // kernel params + launch shape of the captured graph
+  std::map<std::string, std::shared_ptr<JitModule>> modules;
+};
+
+std::mutex g_bmu;
+std::map<const linon_ctx*, BatchState> g_batch;
+
+std::string batch_module_source(const std::vector<const linon_field*>& fields) {
+  std::ostringstream s;
+  s << "#include \"march.cuh\"\n";
+  for (size_t i = 0; i < fields.size(); ++i) {
+    std::string code = fields[i]->cuda;
+    // rename the namespace of each field
+    const std::string from = "namespace linon_user {";
+    size_t p = code.find(from);
+    if (p != std::string::npos) code.replace(p, from.size(), "namespace linon_user_" + std::to_string(i) + " {");
+    s << code;
+  }
+  s << "struct LinonFields {\n"
+       "  __device__ __forceinline__ wgsl::vec3f operator()(int i, const wgsl::vec3f& pp, const wgsl::vec3f& p,\n"
+       "      const wgsl::vec3f& v0, const wgsl::vec3f& v, float t) const {\n"
+       "    switch (i) {\n";
+  for (size_t i = 1; i < fields.size(); ++i)
+    s << "      case " << i << ": return linon_user_" << i << "::field_function(pp, p, v0, v, t);\n";
+  s << "      default: return linon_user_0::field_function(pp, p, v0, v, t);\n"
+       "    }\n  }\n};\n"
+       "extern \"C\" __global__ void __launch_bounds__(256) linon_batch(linon::BatchArgs a) {\n"
+       "  linon::march_batch_kernel(LinonFields(), a);\n}\n";
+  return s.str();
+}
+
+int dev_grow(linon_ctx* ctx, DevBuf& b, size_t bytes) {
+  if (b.bytes >= bytes && b.p) return LINON_OK;
+  if (ctx->budget && ctx->device_bytes + (bytes - b.bytes) > ctx->budget)
+    return set_error(LINON_ENOMEM, "HBM budget exceeded by the batch tables");
+  if (b.p) {
+    cudaFree(b.p);
+    ctx->device_bytes -= b.bytes;
+  }
+  b.p = nullptr;
+  b.bytes = 0;
+  cudaError_t e = cudaMalloc(&b.p, bytes);
+  if (e != cudaSuccess) return cuda_error(e, "cudaMalloc");
+  b.bytes = bytes;
+  ctx->device_bytes += bytes;
+  return LINON_OK;
+}
+
+int get_module(linon_ctx* ctx, BatchState& bs, const linon_field* const* fields, int32_t n_fields,
+               std::shared_ptr<JitModule>& mod) {
+  std::vector<const linon_field*> fv(fields, fields + n_fields);
+  std::string key;
+  for (auto* f : fv) key += f->cuda + "\x01" + std::to_string(f->flags) + "\x02";
+  auto it = bs.modules.find(key);
+  if (it != bs.modules.end()) {
+    mod = it->second;
+    return LINON_OK;
+  }
+  std::string log;
+  const bool precise = (fv[0]->flags & LINON_COMPILE_PRECISE) != 0;
+  int st = jit_compile(batch_module_source(fv), precise, {"linon_batch"}, mod, log);
+  if (st != LINON_OK) return set_error(st, st == LINON_ECOMPILE ? log : std::string(linon_last_error()));
+  bs.modules[key] = mod;
+  (void)ctx;
+  return LINON_OK;
+}
+
+DevMarch to_dev(const linon_settings& st, const linon_march_params& mp) {
+  DevMarch m;
+  m.h_initial = mp.h_initial;
+  m.t_max = mp.t_max;
+  m.max_steps = mp.max_steps;
+  m.adaptive = mp.adaptive;
+  m.h_fine = mp.h_fine;
+  m.h_fine_above = mp.h_fine_above;
+  m.stop_on_hit = mp.stop_on_hit;
+  m.kahan = mp.kahan;
+  m.focal_length = mp.focal_length;
+  m.viewport_height = mp.viewport_height;
+  m.linear_mode = mp.linear_mode;
+  m.field_weight = st.field_weight;
+  return m;
+}
+
+DevScene scene_of(const linon_ctx* ctx) {
+  DevScene s;
+  const float4* block = static_cast<const float4*>(ctx->scene_block.p);
+  s.nodes = ctx->n_nodes ? block : nullptr;
+  s.tris = block + 2 * size_t(ctx->n_nodes);
+  s.face_rgb = static_cast<const float4*>(ctx->face_rgb.p);
+  s.staged = block;
+  s.n_tris = ctx->n_tris;
+  s.n_nodes = ctx->n_nodes;
+  s.staged_bytes = ctx->staged_bytes;
+  s.pad = 0;
+  return s;
+}
+
+int validate_batch(const linon_ctx* ctx, const linon_field* const* fields, int32_t n_fields,
+                   const linon_view* views, int32_t n_views) {
+  if (!ctx) return set_error(LINON_EINVAL, "null context");
+  if (!fields || n_fields <= 0 || n_fields > LINON_MAX_BATCH_FIELDS)
+    return set_error(LINON_EINVAL, "batch needs 1..8 fields");
+  for (int i = 0; i < n_fields; ++i) {
+    if (!fields[i] || !fields[i]->mod) return set_error(LINON_EINVAL, "null field in batch");
+    if (fields[i]->ctx != ctx) return set_error(LINON_EINVAL, "field belongs to another context");
+    if ((fields[i]->flags & LINON_COMPILE_PRECISE) != (fields[0]->flags & LINON_COMPILE_PRECISE))
+      return set_error(LINON_EINVAL, "all fields of a batch must share the precision flag");
+  }
+  if (!views || n_views <= 0) return set_error(LINON_EINVAL, "batch needs at least one view");
+  if (!ctx->has_scene) return set_error(LINON_ENOSCENE, "render before linon_scene_upload");
+  for (int i = 0; i < n_views; ++i) {
+    const linon_view& v = views[i];
+    if (v.field_index < 0 || v.field_index >= n_fields)
+      return set_error(LINON_EINVAL, "view " + std::to_string(i) + ": field_index out of range");
+    if (v.width <= 0 || v.height <= 0 || v.width > 65535 || v.height > 65535)
+      return set_error(LINON_EINVAL, "view " + std::to_string(i) + ": bad image size");
+    const linon_march_params& p = v.params;
+    if (!(p.h_initial > 0.0f)) return set_error(LINON_EINVAL, "view " + std::to_string(i) + ": h_initial must be positive");
+    if (p.max_steps < 0 || p.max_steps > 50000000)
+      return set_error(LINON_EINVAL, "view " + std::to_string(i) + ": max_steps out of range");
+    if (p.max_steps == 0) {
+      float hmin = p.adaptive ? std::min(p.h_initial, p.h_fine) : p.h_initial;
+      if (!(hmin > 0.0f) || double(p.t_max) / hmin > 5e7 || std::fabs(p.t_max) + hmin == std::fabs(p.t_max))
+        return set_error(LINON_EINVAL, "view " + std::to_string(i) + ": t-loop would not terminate");
+    }
+  }
+  return LINON_OK;
+}
+
+}  // namespace
+
+void batch_release(linon_ctx* ctx) {
+  std::lock_guard<std::mutex> lock(g_bmu);
+  auto it = g_batch.find(ctx);
+  if (it == g_batch.end()) return;
+  BatchState& bs = it->second;
+  if (bs.exec) cudaGraphExecDestroy(bs.exec);
+  if (bs.graph) cudaGraphDestroy(bs.graph);
+  if (bs.views.p) cudaFree(bs.views.p);
+  if (bs.counter.p) cudaFree(bs.counter.p);
+  g_batch.erase(it);
+}
+
+}  // namespace linon
+
+using namespace linon;
+
+extern "C" {
+
+int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fields,
+                       const linon_view* views, int32_t n_views, const linon_batch_tuning* tuning) {
+  try {
+    if (int st = validate_batch(ctx, fields, n_fields, views, n_views)) return st;
+    LINON_CUDA(cudaSetDevice(ctx->device));
+    std::lock_guard<std::mutex> lock(g_bmu);
+    BatchState& bs = g_batch[ctx];
+    std::shared_ptr<JitModule> mod;
+    if (int st = get_module(ctx, bs, fields, n_fields, mod)) return st;
+    linon_batch_tuning t{};
+    if (tuning) t = *tuning;
+    else if (ctx->has_tuned) t = ctx->tuned;
+    if (t.quantum <= 0) t.quantum = 32;
+    if (t.block_threads <= 0) t.block_threads = 128;
+    if (t.block_threads % 32 || t.block_threads > 256) return set_error(LINON_EINVAL, "block_threads must be a multiple of 32, <= 256");
+    if (t.tile_w <= 0 || t.tile_h <= 0) { t.tile_w = 8; t.tile_h = 4; }
+    if (t.tile_w * t.tile_h != 32) return set_error(LINON_EINVAL, "tile_w * tile_h must be 32");
+    // view table
+    std::vector<BatchView> tab(static_cast<size_t>(n_views));
+    long long begin = 0;
+    for (int i = 0; i < n_views; ++i) {
+      const linon_view& v = views[i];
+      BatchView& b = tab[size_t(i)];
+      b.m = to_dev(v.settings, v.params);
+      for (int k = 0; k < 3; ++k) {
+        b.cam.o[k] = v.camera.origin[k];
+        b.cam.d[k] = v.camera.view_direction[k];
+        b.cam.u[k] = v.camera.up[k];
+      }
+      b.field = v.field_index;
+      b.tiles_x = (v.width + t.tile_w - 1) / t.tile_w;
+      const int tiles_y = (v.height + t.tile_h - 1) / t.tile_h;
+      b.ray_begin = begin;
+      b.frame.W = v.width;
+      b.frame.H = v.height;
+      b.frame.color = reinterpret_cast<uchar4*>(v.out.color);
+      b.frame.mapping = reinterpret_cast<float4*>(v.out.mapping);
+      b.frame.hit = v.out.hit_id;
+      b.frame.steps = v.out.steps;
+      begin += (long long)b.tiles_x * tiles_y * 32;
+    }
+    if (int st = dev_grow(ctx, bs.views, sizeof(BatchView) * tab.size())) return st;
+    if (int st = dev_grow(ctx, bs.counter, 256)) return st;
+    LINON_CUDA(cudaMemcpyAsync(bs.views.p, tab.data(), sizeof(BatchView) * tab.size(),
+                               cudaMemcpyHostToDevice, ctx->stream));
+    BatchArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.views = static_cast<const BatchView*>(bs.views.p);
+    a.n_views = n_views;
+    a.quantum = t.quantum;
+    a.total_rays = begin;
+    a.counter = static_cast<unsigned long long*>(bs.counter.p);
+    a.scene = scene_of(ctx);
+    a.tile_w = t.tile_w;
+    a.tile_h = t.tile_h;
+    a.err = ctx->d_err;
+    cudaKernel_t k = mod->kernels.at("linon_batch");
+    int sms = 0;
+    LINON_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    int per_sm = t.ctas_per_sm;
+    if (per_sm <= 0) {
+      int occ = 0;
+      LINON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)k, t.block_threads,
+                                                               size_t(a.scene.staged_bytes)));
+      per_sm = std::max(1, occ);
+    }
+    const dim3 grid(unsigned(sms * per_sm)), block(unsigned(t.block_threads));
+    // graph key: the kernel parameters and the launch shape
+    std::vector<char> key(sizeof a + sizeof(k) + 2 * sizeof(unsigned));
+    std::memcpy(key.data(), &a, sizeof a);
+    std::memcpy(key.data() + sizeof a, &k, sizeof k);
+    std::memcpy(key.data() + sizeof a + sizeof k, &grid.x, sizeof(unsigned));
+    std::memcpy(key.data() + sizeof a + sizeof k + sizeof(unsigned), &block.x, sizeof(unsigned));
+    if (!bs.exec || key != bs.key) {
+      if (bs.exec) { cudaGraphExecDestroy(bs.exec); bs.exec = nullptr; }
+      if (bs.graph) { cudaGraphDestroy(bs.graph); bs.graph = nullptr; }
+      cudaStream_t cs;
+      LINON_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+      LINON_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+      cudaMemsetAsync(bs.counter.p, 0, sizeof(unsigned long long), cs);
+      void* args[] = {&a};
+      cudaError_t le = cudaLaunchKernel((const void*)k, grid, block, args, size_t(a.scene.staged_bytes), cs);
+      cudaError_t ce = cudaStreamEndCapture(cs, &bs.graph);
+      cudaStreamDestroy(cs);
+      if (le != cudaSuccess) return cuda_error(le, "cudaLaunchKernel (capture)");
+      if (ce != cudaSuccess) return cuda_error(ce, "cudaStreamEndCapture");
+      LINON_CUDA(cudaGraphInstantiate(&bs.exec, bs.graph, 0));
+      bs.key = key;
+    }
+    LINON_CUDA(cudaGraphLaunch(bs.exec, ctx->stream));
+    return LINON_OK;
+  } catch (const std::exception& e) {
+    return set_error(LINON_EINVAL, std::string("internal error: ") + e.what());
+  }
+}
+
+int linon_render_views_plain(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fields,
+                             const linon_view* views, int32_t n_views) {
+  if (int st = validate_batch(ctx, fields, n_fields, views, n_views)) return st;
+  for (int i = 0; i < n_views; ++i) {
+    const linon_view& v = views[i];
+    linon_frame f = v.out;
+    f.width = v.width;
+    f.height = v.height;
+    if (int st = linon_render(ctx, fields[v.field_index], &v.camera, &v.settings, &v.params, &f)) return st;
+  }
+  return LINON_OK;
+}
+
+int linon_autotune_batch(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fields,
+                         const linon_view* views, int32_t n_views, linon_batch_tuning* best,
+                         double* best_ms) {
+  if (int st = validate_batch(ctx, fields, n_fields, views, n_views)) return st;
+  const int quanta[] = {8, 16, 32, 64};
+  const int blocks[] = {64, 128, 256};
+  const int tiles[][2] = {{8, 4}, {4, 8}, {16, 2}};
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best_t = 1e300;
+  linon_batch_tuning bt{};
+  for (int q : quanta)
+    for (int b : blocks)
+      for (auto& tl : tiles) {
+        linon_batch_tuning t{};
+        t.quantum = q;
+        t.block_threads = b;
+        t.tile_w = tl[0];
+        t.tile_h = tl[1];
+        if (int st = linon_render_batch(ctx, fields, n_fields, views, n_views, &t)) {
+          cudaEventDestroy(e0);
+          cudaEventDestroy(e1);
+          return st;
+        }
+        cudaEventRecord(e0, ctx->stream);
+        int st = linon_render_batch(ctx, fields, n_fields, views, n_views, &t);
+        cudaEventRecord(e1, ctx->stream);
+        if (st) {
+          cudaEventDestroy(e0);
+          cudaEventDestroy(e1);
+          return st;
+        }
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_t) {
+          best_t = ms;
+          bt = t;
+        }
+      }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->tuned = bt;
+  ctx->has_tuned = true;
+  if (best) *best = bt;
+  if (best_ms) *best_ms = best_t;
+  return LINON_OK;
+}
+
+}  // extern "C"

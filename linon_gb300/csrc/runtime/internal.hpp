@@ -1,0 +1,103 @@
+// internal.hpp — shared declarations of the linon runtime (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../../include/linon.h"
+#include "../device/march_types.h"
+
+namespace linon {
+
+// ---- errors -------------------------------------------------------------
+int set_error(int status, const std::string& msg);
+int cuda_error(cudaError_t e, const char* what);
+#define LINON_CUDA(call)                                      \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return ::linon::cuda_error(e_, #call); \
+  } while (0)
+
+// ---- device memory owned by a context -----------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+// ---- embedded device sources (generated at build time) -------------------
+struct EmbeddedFile {
+  const char* name;
+  const char* text;
+};
+extern const EmbeddedFile kEmbeddedDeviceSources[];
+extern const int kEmbeddedDeviceSourceCount;
+
+// ---- NVRTC JIT ----------------------------------------------------------
+// One compiled module: the march kernels of one or several fields.
+struct JitModule {
+  cudaLibrary_t lib = nullptr;
+  std::map<std::string, cudaKernel_t> kernels;
+  std::string key;
+  double compile_ms = 0;
+};
+// Compiles `source` (which #includes the embedded headers) for sm_103a and
+// loads it on the current device.  Results are cached per (source, options)
+// in memory and, when LINON_CACHE_DIR is set, on disk.
+int jit_compile(const std::string& source, bool precise, const std::vector<std::string>& kernel_names,
+                std::shared_ptr<JitModule>& out, std::string& log);
+// Compiles `source` to a cubin without loading it (no device needed); the
+// log carries the compiler's and ptxas' messages (registers, spills).
+int jit_check(const std::string& source, bool precise, std::string& log, size_t* cubin_bytes);
+
+// ---- BVH ----------------------------------------------------------------
+struct BvhBuild {
+  std::vector<float4> nodes;   // 2 per node
+  std::vector<float4> tris;    // 3 per triangle, leaf order
+  uint32_t max_depth = 0;
+};
+// Builds the triangle array (brute force when leaf_size == 0) and, when
+// requested, a binned-SAH BVH whose node boxes are inflated by `margin`.
+void build_scene_arrays(const float* xyz, uint32_t nv, const uint32_t* abc, uint32_t nf,
+                        bool bvh, BvhBuild& out);
+
+// Frees the batch tables, graphs and modules of a context (batch.cpp).
+void batch_release(linon_ctx* ctx);
+
+}  // namespace linon
+
+// ---- context and field objects (opaque in the ABI) ----------------------
+struct linon_field {
+  linon_ctx* ctx = nullptr;
+  std::string body, helpers, cuda;
+  int flags = 0;
+  int flops_arith = 0, flops_transc = 0;
+  std::shared_ptr<linon::JitModule> mod;
+};
+
+struct linon_ctx {
+  int device = 0;
+  size_t budget = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  size_t device_bytes = 0;
+  // scene
+  bool has_scene = false;
+  linon::DevBuf scene_block;  // [nodes | tris]
+  linon::DevBuf face_rgb;
+  int n_tris = 0, n_nodes = 0;
+  uint32_t max_depth = 0;
+  int staged_bytes = 0;
+  // device error word and scratch
+  int* d_err = nullptr;
+  linon::DevBuf scratch;       // grown on demand (capture positions, queues, ...)
+  linon::DevBuf host_io;       // device planes for linon_render_host
+  // batch tuning cache
+  linon_batch_tuning tuned{};
+  bool has_tuned = false;
+};

@@ -1,0 +1,314 @@
+// kernels.cu — ahead-of-time kernels that do not depend on the field
+// function: the Lyapunov overlay (src/overlay.wgsl), the finite-time exponent,
+// outline-ray selection (src/main_view.wgsl:381-468), exponent quantiles,
+// RaySample packing (src/main_view.wgsl:290-309) and an FP32 throughput probe.
+//
+// Compiled with -fmad=false so that the FP32 overlay is op-for-op the
+// shader's arithmetic (no contraction), like the FP32 restatement.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../device/march_types.h"
+#include "../device/wgsl_rt.cuh"
+#include "kernels.hpp"
+
+namespace linon {
+namespace {
+
+__device__ __forceinline__ unsigned char unorm8(float x) {
+  float c = fminf(fmaxf(x, 0.0f), 1.0f);
+  return (unsigned char)__float2uint_rn(c * 255.0f);
+}
+
+__device__ __forceinline__ float srgb_from_linear(float c) {  // overlay.wgsl:148-154
+  if (c < 0.0031308f) return c / 12.92f;
+  return 1.055f * powf(c, 1.0f / 2.4f) - 0.055f;
+}
+
+// lyapunov_exponent, overlay.wgsl:99-112 with mat2eigenvalues (:4-40)
+template <class T>
+__device__ __forceinline__ T lyapunov(const float4* mapping, int W, int x, int y, int delta) {
+  auto ld = [&](int xx, int yy, T& a, T& b, T& c) {
+    const float4 q = mapping[size_t(yy) * W + xx];
+    a = T(q.x);
+    b = T(q.y);
+    c = T(q.z);
+  };
+  T xn0, xn1, xn2, xp0, xp1, xp2, yn0, yn1, yn2, yp0, yp1, yp2;
+  ld(x + delta, y, xn0, xn1, xn2);
+  ld(x - delta, y, xp0, xp1, xp2);
+  ld(x, y + delta, yn0, yn1, yn2);
+  ld(x, y - delta, yp0, yp1, yp2);
+  const T half = T(0.5);
+  const T g00 = half * (xn0 - xp0), g01 = half * (xn1 - xp1), g02 = half * (xn2 - xp2);
+  const T g10 = half * (yn0 - yp0), g11 = half * (yn1 - yp1), g12 = half * (yn2 - yp2);
+  const T m00 = (g00 * g00 + g01 * g01) + g02 * g02;
+  const T m01 = (g00 * g10 + g01 * g11) + g02 * g12;
+  const T m10 = (g10 * g00 + g11 * g01) + g12 * g02;
+  const T m11 = (g10 * g10 + g11 * g11) + g12 * g12;
+  const T a0 = m00 * m11 - m01 * m10;
+  const T a1 = -(m00 + m11);
+  const T discrim = a1 * a1 - T(4.0) * a0;
+  T e0, e1;
+  if (discrim >= T(0.0)) {
+    const T root = sqrt(discrim);
+    e0 = (-a1 - root) / T(2.0);
+    e1 = (-a1 + root) / T(2.0);
+  } else {
+    const T root = sqrt(-discrim);
+    e0 = -a1 / T(2.0);
+    e1 = root / T(2.0);
+  }
+  return sqrt(fmax(e0, e1));
+}
+
+template <bool FP64>
+__global__ void overlay_kernel(OverlayArgs a) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= a.W || y >= a.H) return;
+  const size_t idx = size_t(y) * a.W + x;
+  const uchar4 c8 = a.in[idx];
+  float c[4] = {c8.x / 255.0f, c8.y / 255.0f, c8.z / 255.0f, c8.w / 255.0f};
+  const int padding = a.delta * 2;
+  if (a.mode != 0 && !(x < padding || y < padding || x >= a.W - padding || y >= a.H - padding) &&
+      a.mode == 1) {
+    float scaled;
+    if (FP64) {
+      double e = lyapunov<double>(a.mapping, a.W, x, y, a.delta);
+      scaled = float(exp(double(a.scaling) * e - 5.0));
+    } else {
+      float e = lyapunov<float>(a.mapping, a.W, x, y, a.delta);
+      scaled = expf(a.scaling * e - 5.0f);
+    }
+    if (a.exponents) a.exponents[idx] = scaled;
+    if (scaled >= 0.8f) {
+      const float alpha = fminf(1.0f, scaled) * 0.5f;
+      for (int i = 0; i < 4; ++i) c[i] = alpha * 1.0f + (1.0f - alpha) * c[i];
+    }
+  }
+  if (a.srgb)
+    for (int i = 0; i < 3; ++i) c[i] = srgb_from_linear(c[i]);
+  a.out[idx] = make_uchar4(unorm8(c[0]), unorm8(c[1]), unorm8(c[2]), unorm8(c[3]));
+}
+
+// Primary direction in FP32, the march kernel's formula (main_view.wgsl:347-366).
+struct DirBasis {
+  float nh[3], nv[3], d[3];
+  float width, height, vw, vh, focal;
+};
+
+__device__ __forceinline__ void primary_dir(const DirBasis& b, int gx, int gy, float out[3]) {
+  float u = float(gx) / (b.width - 1.0f) * b.vw - 0.5f * b.vw;
+  float v = float(gy) / (b.height - 1.0f) * b.vh - 0.5f * b.vh;
+  float s[3];
+  for (int k = 0; k < 3; ++k) s[k] = (u * b.nh[k] + v * b.nv[k]) + b.focal * b.d[k];
+  float l = sqrtf((s[0] * s[0] + s[1] * s[1]) + s[2] * s[2]);
+  for (int k = 0; k < 3; ++k) out[k] = s[k] / l;
+}
+
+__global__ void ftle_kernel(FtleArgs a) {
+  __shared__ DirBasis b;
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    wgsl::vec3f d(a.cam.d[0], a.cam.d[1], a.cam.d[2]), up(a.cam.u[0], a.cam.u[1], a.cam.u[2]);
+    b.width = float(a.W);
+    b.height = float(a.H);
+    const float aspect = b.width / b.height;
+    b.focal = a.focal_length;
+    b.vh = a.viewport_height;
+    b.vw = aspect * b.vh;
+    wgsl::vec3f w = -d;
+    wgsl::vec3f hor = wgsl::cross(up, w);
+    wgsl::vec3f ver = wgsl::cross(w, hor);
+    float lh = sqrtf(wgsl::dot(hor, hor)), lv = sqrtf(wgsl::dot(ver, ver));
+    b.nh[0] = hor.x / lh; b.nh[1] = hor.y / lh; b.nh[2] = hor.z / lh;
+    b.nv[0] = ver.x / lv; b.nv[1] = ver.y / lv; b.nv[2] = ver.z / lv;
+    b.d[0] = d.x; b.d[1] = d.y; b.d[2] = d.z;
+  }
+  __syncthreads();
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= a.W || y >= a.H) return;
+  const size_t ci = size_t(y) * a.W + x;
+  float dc[3];
+  primary_dir(b, x, a.H - 1 - y, dc);
+  const float4 ec = a.mapping[ci];
+  const int dx[4] = {1, -1, 0, 0}, dy[4] = {0, 0, 1, -1};
+  double best = -1.0;
+  for (int k = 0; k < 4; ++k) {
+    const int nx = x + dx[k], ny = y + dy[k];
+    if (nx < 0 || ny < 0 || nx >= a.W || ny >= a.H) continue;
+    const float4 en = a.mapping[size_t(ny) * a.W + nx];
+    float dn[3];
+    primary_dir(b, nx, a.H - 1 - ny, dn);
+    const double e0 = double(en.x) - double(ec.x), e1 = double(en.y) - double(ec.y),
+                 e2 = double(en.z) - double(ec.z);
+    const double q0 = double(dn[0]) - double(dc[0]), q1 = double(dn[1]) - double(dc[1]),
+                 q2 = double(dn[2]) - double(dc[2]);
+    const double de = (e0 * e0 + e1 * e1) + e2 * e2;
+    const double dd = (q0 * q0 + q1 * q1) + q2 * q2;
+    const double r = sqrt(de) / sqrt(dd);
+    if (r > best) best = r;
+  }
+  a.out[ci] = best > 0.0 ? float(log(best) / a.T) : -__int_as_float(0x7f800000);
+}
+
+// Outline selection.  Each of the shader's 8 scans picks either the last
+// pixel in its scan order with the largest score (corner scans, `>=`) or the
+// first pixel in its scan order (edge scans, `found`).  Both are reductions:
+// keys (score << 32 | scan position) under atomicMax, or scan positions under
+// atomicMin.  slots[0..7] hold the keys; the host decodes them.
+__global__ void outline_kernel(const float* e, int W, int H, float min_exp,
+                               unsigned long long* slots) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  bool ok = x < W && y < H && e[size_t(y) * W + x] >= min_exp;
+  unsigned long long k[8];
+  if (ok) {
+    const unsigned long long colpos = (unsigned long long)x * H + y;  // x outer, y inner
+    k[0] = ((unsigned long long)((W - x) + y) << 32) | colpos;        // bottom left
+    k[2] = ((unsigned long long)(x + y) << 32) | colpos;              // bottom right
+    k[4] = ((unsigned long long)(x + (H - y)) << 32) | colpos;        // top right
+    k[6] = ((unsigned long long)((W - x) + (H - y)) << 32) | colpos;  // top left
+    // bottom middle: y from W-1 down (rows >= H never exist), x up
+    k[1] = (y < W) ? (unsigned long long)(W - 1 - y) * W + x : ~0ull;
+    k[3] = (unsigned long long)(W - 1 - x) * H + y;                   // middle right
+    k[5] = (unsigned long long)y * W + x;                             // top middle
+    k[7] = colpos;                                                    // middle left
+  }
+  const unsigned mask = __ballot_sync(0xffffffffu, ok);
+  if (mask == 0) return;
+  for (int g = 0; g < 8; ++g) {
+    const bool maxred = (g % 2) == 0;
+    unsigned long long v = ok ? k[g] : (maxred ? 0ull : ~0ull);
+    for (int off = 16; off > 0; off >>= 1) {
+      unsigned long long o = __shfl_down_sync(0xffffffffu, v, off);
+      v = maxred ? (o > v ? o : v) : (o < v ? o : v);
+    }
+    if ((threadIdx.x + threadIdx.y * blockDim.x) % 32 == 0) {
+      if (maxred) atomicMax(&slots[g], v);
+      else atomicMin(&slots[g], v);
+    }
+  }
+  if ((threadIdx.x + threadIdx.y * blockDim.x) % 32 == 0) atomicAdd(&slots[8], 1ull);
+}
+
+__global__ void outline_init_kernel(unsigned long long* slots) {
+  const int g = threadIdx.x;
+  if (g < 8) slots[g] = (g % 2) == 0 ? 0ull : ~0ull;
+  if (g == 8) slots[8] = 0ull;
+}
+
+// Order-preserving key of a float (NaN sorts last).
+__device__ __forceinline__ unsigned fkey(float f) {
+  unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// Radix-select histogram pass over the interior pixels: counts keys whose
+// bits above `shift+bits` equal `prefix`, binned by the next `bits` bits.
+__global__ void quantile_hist_kernel(const float* e, int W, int H, int border, unsigned prefix,
+                                     int high_shift, int shift, int bits, unsigned* hist) {
+  extern __shared__ unsigned sh[];
+  const int nb = 1 << bits;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  const int iw = W - 2 * border, ih = H - 2 * border;
+  const long long n = (long long)iw * ih;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int x = int(i % iw) + border, y = int(i / iw) + border;
+    const unsigned k = fkey(e[size_t(y) * W + x]);
+    if (high_shift < 32 && (k >> high_shift) != prefix) continue;
+    atomicAdd(&sh[(k >> shift) & (nb - 1)], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+// RaySample packing: positions + sample_colors (main_view.wgsl:326-335).
+__global__ void pack_samples_kernel(const float4* pos, linon_ray_sample* out, int n_rays,
+                                    int n_pts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_rays * n_pts) return;
+  const int ray = i / n_pts;
+  const float cols[8][3] = {{1.0f, 0.0f, 0.0f}, {0.5f, 0.5f, 0.0f}, {0.0f, 1.0f, 0.0f},
+                            {0.5f, 1.0f, 0.0f}, {1.0f, 1.0f, 0.0f}, {0.5f, 0.5f, 0.5f},
+                            {0.0f, 0.0f, 1.0f}, {0.5f, 0.0f, 0.5f}};
+  const float4 p = pos[i];
+  linon_ray_sample s;
+  s.position[0] = p.x;
+  s.position[1] = p.y;
+  s.position[2] = p.z;
+  s.position[3] = 1.0f;
+  s.color[0] = cols[ray & 7][0];
+  s.color[1] = cols[ray & 7][1];
+  s.color[2] = cols[ray & 7][2];
+  s.color[3] = 0.5f;
+  out[i] = s;
+}
+
+// FP32 throughput probe: independent FFMA chains per thread.
+__global__ void fp32_probe_kernel(float* out, int iters, float seed) {
+  float a0 = seed + threadIdx.x, a1 = a0 + 1.0f, a2 = a0 + 2.0f, a3 = a0 + 3.0f;
+  float a4 = a0 + 4.0f, a5 = a0 + 5.0f, a6 = a0 + 6.0f, a7 = a0 + 7.0f;
+  const float m = 0.9999999f, c = 1e-7f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      a0 = fmaf(a0, m, c); a1 = fmaf(a1, m, c); a2 = fmaf(a2, m, c); a3 = fmaf(a3, m, c);
+      a4 = fmaf(a4, m, c); a5 = fmaf(a5, m, c); a6 = fmaf(a6, m, c); a7 = fmaf(a7, m, c);
+    }
+  }
+  const float s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+  if (s == 12345.678f) out[0] = s;  // keeps the chains alive
+}
+
+}  // namespace
+
+cudaError_t launch_overlay(const OverlayArgs& a, bool fp64, cudaStream_t s) {
+  dim3 block(16, 8), grid((a.W + 15) / 16, (a.H + 7) / 8);
+  if (fp64) overlay_kernel<true><<<grid, block, 0, s>>>(a);
+  else overlay_kernel<false><<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ftle(const FtleArgs& a, cudaStream_t s) {
+  dim3 block(16, 8), grid((a.W + 15) / 16, (a.H + 7) / 8);
+  ftle_kernel<<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_outline(const float* e, int W, int H, float min_exp, unsigned long long* slots,
+                           cudaStream_t s) {
+  outline_init_kernel<<<1, 32, 0, s>>>(slots);
+  dim3 block(32, 8), grid((W + 31) / 32, (H + 7) / 8);
+  outline_kernel<<<grid, block, 0, s>>>(e, W, H, min_exp, slots);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_quantile_hist(const float* e, int W, int H, int border, unsigned prefix,
+                                 int high_shift, int shift, int bits, unsigned* hist,
+                                 cudaStream_t s) {
+  const int nb = 1 << bits;
+  cudaError_t err = cudaMemsetAsync(hist, 0, sizeof(unsigned) * nb, s);
+  if (err != cudaSuccess) return err;
+  quantile_hist_kernel<<<152 * 4, 256, sizeof(unsigned) * nb, s>>>(e, W, H, border, prefix,
+                                                                    high_shift, shift, bits, hist);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_samples(const float4* pos, linon_ray_sample* out, int n_rays, int n_pts,
+                                cudaStream_t s) {
+  const int n = n_rays * n_pts;
+  pack_samples_kernel<<<(n + 255) / 256, 256, 0, s>>>(pos, out, n_rays, n_pts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fp32_probe(float* out, int blocks, int threads, int iters, cudaStream_t s) {
+  fp32_probe_kernel<<<blocks, threads, 0, s>>>(out, iters, 1.0f);
+  return cudaGetLastError();
+}
+
+}  // namespace linon

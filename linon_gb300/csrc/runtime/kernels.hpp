@@ -1,0 +1,43 @@
+// kernels.hpp — host launchers of the ahead-of-time kernels in kernels.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../../include/linon.h"
+#include "../device/march_types.h"
+
+namespace linon {
+
+struct OverlayArgs {
+  const uchar4* in;       // ray-casting image (rgba8)
+  const float4* mapping;  // endpoints
+  uchar4* out;            // target image
+  float* exponents;       // W*H, may be NULL
+  int W, H;
+  int mode, delta;
+  float scaling;
+  int srgb;
+};
+
+struct FtleArgs {
+  DevCamera cam;
+  const float4* mapping;
+  float* out;
+  int W, H;
+  float focal_length, viewport_height;
+  double T;
+};
+
+cudaError_t launch_overlay(const OverlayArgs& a, bool fp64, cudaStream_t s);
+cudaError_t launch_ftle(const FtleArgs& a, cudaStream_t s);
+// slots: 9 u64 (8 selection keys + a found counter)
+cudaError_t launch_outline(const float* e, int W, int H, float min_exp, unsigned long long* slots,
+                           cudaStream_t s);
+cudaError_t launch_quantile_hist(const float* e, int W, int H, int border, unsigned prefix,
+                                 int high_shift, int shift, int bits, unsigned* hist,
+                                 cudaStream_t s);
+cudaError_t launch_pack_samples(const float4* pos, linon_ray_sample* out, int n_rays, int n_pts,
+                                cudaStream_t s);
+cudaError_t launch_fp32_probe(float* out, int blocks, int threads, int iters, cudaStream_t s);
+
+}  // namespace linon

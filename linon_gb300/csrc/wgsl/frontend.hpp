@@ -1,0 +1,32 @@
+// frontend.hpp — WGSL-subset front end: field-function source -> CUDA C.
+//
+// Replaces the naga path of the reference (src/main_view.rs:649-690, which
+// splices the user body into the shader with with_field_function,
+// src/main_view.rs:852-861, and lets naga parse and validate it).  The input
+// is the body of
+//   fn field_function(p_prev: vec3<f32>, p: vec3<f32>, v0: vec3<f32>,
+//                     v: vec3<f32>, t: f32) -> vec3<f32>
+// plus optional module-scope helper functions and constants.  The output is
+// CUDA C written against device/wgsl_rt.cuh.
+#pragma once
+
+#include <string>
+
+namespace linon {
+namespace wgslfe {
+
+struct Translation {
+  bool ok = false;
+  std::string code;      // CUDA C: namespace <ns> { ... field_function ... }
+  std::string log;       // diagnostics (errors) when !ok
+  int flops_arith = 0;   // counted FP32 add/mul/div/sqrt of one evaluation
+  int flops_transc = 0;  // transcendental calls of one evaluation
+};
+
+// ns: C++ namespace that receives the generated functions; the field is
+// ns::field_function(vec3f p_prev, vec3f p, vec3f v0, vec3f v, float t).
+Translation translate(const std::string& field_body, const std::string& helpers_src,
+                      const std::string& ns);
+
+}  // namespace wgslfe
+}  // namespace linon

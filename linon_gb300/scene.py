@@ -1,0 +1,155 @@
+"""Scene inputs: the Cornell box, vertex normalisation, icospheres.
+
+The Cornell box is the public Cornell Program of Computer Graphics
+measurement set, in the vertex/face order of src/cornell_box.rs:1-163 (18
+quads, two triangles each, so face indices match the reference's).  The
+preparation of src/application.rs:105-123 (negate x and z, then one global
+min/max normalisation, src/vertices.rs:3-17) and the bounding-box centre of
+src/vertices.rs:19-57 are restated in float32 arithmetic.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+# Quads as (name, 4 vertices); each becomes triangles (a,b,c), (c,d,a),
+# the index pattern of src/cornell_box.rs:102-163.
+CORNELL_QUADS = [
+    ("floor", [(552.8, 0.0, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, 559.2), (549.6, 0.0, 559.2)]),
+    ("floor", [(130.0, 0.0, 65.0), (82.0, 0.0, 225.0), (240.0, 0.0, 272.0), (290.0, 0.0, 114.0)]),
+    ("floor", [(423.0, 0.0, 247.0), (265.0, 0.0, 296.0), (314.0, 0.0, 456.0), (472.0, 0.0, 406.0)]),
+    ("ceiling", [(556.0, 548.8, 0.0), (556.0, 548.8, 559.2), (0.0, 548.8, 559.2), (0.0, 548.8, 0.0)]),
+    ("light", [(343.0, 548.8, 227.0), (343.0, 548.8, 332.0), (213.0, 548.8, 332.0), (213.0, 548.8, 227.0)]),
+    ("back", [(549.6, 0.0, 559.2), (0.0, 0.0, 559.2), (0.0, 548.8, 559.2), (556.0, 548.8, 559.2)]),
+    ("green", [(0.0, 0.0, 559.2), (0.0, 0.0, 0.0), (0.0, 548.8, 0.0), (0.0, 548.8, 559.2)]),
+    ("red", [(552.8, 0.0, 0.0), (549.6, 0.0, 559.2), (556.0, 548.8, 559.2), (556.0, 548.8, 0.0)]),
+    ("short", [(130.0, 165.0, 65.0), (82.0, 165.0, 225.0), (240.0, 165.0, 272.0), (290.0, 165.0, 114.0)]),
+    ("short", [(290.0, 0.0, 114.0), (290.0, 165.0, 114.0), (240.0, 165.0, 272.0), (240.0, 0.0, 272.0)]),
+    ("short", [(130.0, 0.0, 65.0), (130.0, 165.0, 65.0), (290.0, 165.0, 114.0), (290.0, 0.0, 114.0)]),
+    ("short", [(82.0, 0.0, 225.0), (82.0, 165.0, 225.0), (130.0, 165.0, 65.0), (130.0, 0.0, 65.0)]),
+    ("short", [(240.0, 0.0, 272.0), (240.0, 165.0, 272.0), (82.0, 165.0, 225.0), (82.0, 0.0, 225.0)]),
+    ("tall", [(423.0, 330.0, 247.0), (265.0, 330.0, 296.0), (314.0, 330.0, 456.0), (472.0, 330.0, 406.0)]),
+    ("tall", [(423.0, 0.0, 247.0), (423.0, 330.0, 247.0), (472.0, 330.0, 406.0), (472.0, 0.0, 406.0)]),
+    ("tall", [(472.0, 0.0, 406.0), (472.0, 330.0, 406.0), (314.0, 330.0, 456.0), (314.0, 0.0, 456.0)]),
+    ("tall", [(314.0, 0.0, 456.0), (314.0, 330.0, 456.0), (265.0, 330.0, 296.0), (265.0, 0.0, 296.0)]),
+    ("tall", [(265.0, 0.0, 296.0), (265.0, 330.0, 296.0), (423.0, 330.0, 247.0), (423.0, 0.0, 247.0)]),
+]
+
+# Diffuse reflectances of the published Cornell box (white / red / green).
+_WHITE = (0.725, 0.71, 0.68)
+_RGB = {"red": (0.63, 0.065, 0.05), "green": (0.14, 0.45, 0.091), "light": (1.0, 1.0, 1.0)}
+
+
+def cornell_raw():
+    """Raw Cornell box: (vertices float32 [72,3], faces uint32 [36,3], face_rgb float32 [36,3])."""
+    verts, faces, rgb = [], [], []
+    for q, (name, quad) in enumerate(CORNELL_QUADS):
+        verts.extend(quad)
+        b = 4 * q
+        faces.append((b, b + 1, b + 2))
+        faces.append((b + 2, b + 3, b))
+        c = _RGB.get(name, _WHITE)
+        rgb.extend([c, c])
+    return (np.asarray(verts, dtype=np.float32), np.asarray(faces, dtype=np.uint32),
+            np.asarray(rgb, dtype=np.float32))
+
+
+def normalize_vertices(v: np.ndarray) -> np.ndarray:
+    """src/vertices.rs:3-17: one global min/max over all coordinates, float32 ops."""
+    v = np.asarray(v, dtype=np.float32)
+    lo, hi = np.float32(v.min()), np.float32(v.max())
+    out = (v - lo) / (hi - lo)
+    return (out * np.float32(2.0) - np.float32(1.0)).astype(np.float32)
+
+
+def normalize_per_axis(v: np.ndarray) -> np.ndarray:
+    """Per-axis min/max normalisation to [-1,1]^3 (float32 ops)."""
+    v = np.asarray(v, dtype=np.float32)
+    lo, hi = v.min(axis=0), v.max(axis=0)
+    out = (v - lo) / (hi - lo)
+    return (out * np.float32(2.0) - np.float32(1.0)).astype(np.float32)
+
+
+def get_center(v: np.ndarray) -> np.ndarray:
+    """src/vertices.rs:19-57: centre of the axis-aligned bounding box (float32)."""
+    v = np.asarray(v, dtype=np.float32).reshape(-1, 3)
+    return ((v.min(axis=0) + v.max(axis=0)) / np.float32(2.0)).astype(np.float32)
+
+
+def cornell_reference():
+    """The scene the reference application builds (src/application.rs:105-123):
+    x and z negated, then normalize_vertices.  Returns (xyz, faces, face_rgb, center)."""
+    v, f, rgb = cornell_raw()
+    v = v.copy()
+    v[:, 0] = -v[:, 0]
+    v[:, 2] = -v[:, 2]
+    v = normalize_vertices(v)
+    return v, f, rgb, get_center(v)
+
+
+def cornell_unit():
+    """The Cornell room of the benchmark workloads: x and z negated (open side
+    facing +z), each axis normalised to [-1,1].  Returns (xyz, faces, face_rgb)."""
+    v, f, rgb = cornell_raw()
+    v = v.copy()
+    v[:, 0] = -v[:, 0]
+    v[:, 2] = -v[:, 2]
+    return normalize_per_axis(v), f, rgb
+
+
+def icosphere(subdivisions: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)):
+    """Icosphere by repeated 4-way subdivision of an icosahedron (vertices
+    projected to the sphere).  20 * 4**subdivisions triangles."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t),
+         (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    verts = [np.array(p, dtype=np.float64) / np.linalg.norm(p) for p in v]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4),
+             (11, 10, 2), (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8),
+             (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdivisions):
+        cache = {}
+
+        def mid(a, b):
+            key = (a, b) if a < b else (b, a)
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    xyz = np.asarray(verts) * radius + np.asarray(center, dtype=np.float64)
+    return xyz.astype(np.float32), np.asarray(faces, dtype=np.uint32)
+
+
+def merge(*meshes):
+    """Concatenates (xyz, faces[, rgb]) meshes; faces are re-indexed."""
+    xs, fs, cs = [], [], []
+    base = 0
+    for m in meshes:
+        x, f = m[0], m[1]
+        rgb = m[2] if len(m) > 2 and m[2] is not None else np.full((len(f), 3), 0.8, np.float32)
+        xs.append(x)
+        fs.append(f.astype(np.int64) + base)
+        cs.append(rgb)
+        base += len(x)
+    return (np.concatenate(xs).astype(np.float32), np.concatenate(fs).astype(np.uint32),
+            np.concatenate(cs).astype(np.float32))
+
+
+def cornell_with_spheres(seed: int = 0, n: int = 4, subdivisions: int = 5, radius: float = 0.3):
+    """Cornell room plus n icospheres (20*4**subdivisions triangles each) with
+    centres drawn uniformly inside the room's box shrunk by the radius."""
+    rng = np.random.default_rng(seed)
+    room = cornell_unit()
+    lo, hi = room[0].min(axis=0) + radius, room[0].max(axis=0) - radius
+    meshes = [room]
+    for _ in range(n):
+        c = rng.uniform(lo, hi)
+        x, f = icosphere(subdivisions, radius, c)
+        meshes.append((x, f, np.full((len(f), 3), (0.9, 0.9, 0.95), np.float32)))
+    return merge(*meshes)

@@ -1,0 +1,365 @@
+"""CUDA engine vs the oracle, through the C ABI (GPU).
+
+Bars (written per test):
+  * LINON_COMPILE_PRECISE modules are op-for-op the FP32 restatement: for
+    fields whose arithmetic is + - * / sqrt only, every plane is bit-exact
+    (colour within 1/255: the specular pow is CUDA's powf vs the C library's).
+  * Fields with transcendental calls (CUDA's sinf/expf/powf vs the C
+    library's) agree to FP32 tolerance: hit ids on >= 99% of pixels, endpoint
+    difference small except on the pixels whose hit differs.
+  * Fast modules (FMA contraction) are held to the FP64 oracle: endpoint
+    error <= 1e-4 scene units and hit-id mismatch <= 0.1% on smooth fields.
+  * BVH traversal == brute force (bit-exact, same module).
+"""
+import numpy as np
+import pytest
+import torch
+
+from linon_gb300 import FramePlanes, _abi, camera as cam, scene, workloads as wl
+from linon_gb300.engine import predefined_source
+
+pytestmark = pytest.mark.gpu
+
+EXACT_FIELDS = ["identity", "linear", "lorenz", "roessler", "translation_x", "mirage_spherical", "mirage_plane"]
+TRANSC_FIELDS = ["twist", "rotation", "mirage_spherical_sigmoid", "lens"]
+
+_fields = {}
+
+
+def field(engine, name, precise):
+    key = (name, precise)
+    if key not in _fields:
+        _fields[key] = engine.compile_field(predefined_source(_abi.FIELD_IDS[name]), precise=precise)
+    return _fields[key]
+
+
+def gpu_render(engine, w, fld, width=None, height=None, params=None, settings=None, camera=None):
+    W, H = width or w.width, height or w.height
+    f = FramePlanes.allocate(W, H)
+    engine.render(fld, camera or w.camera, settings or w.settings, params or w.params, f)
+    torch.cuda.synchronize()
+    engine.synchronize()
+    return {k: getattr(f, k).cpu().numpy() for k in ("color", "mapping", "hit_id", "steps")}
+
+
+def oracle_render(oracle, w, fid, width, height, params=None, settings=None, camera=None, precision=32):
+    want = ("color", "mapping", "hit_id", "steps") if precision == 32 else ("mapping64", "hit_id", "steps")
+    return oracle.render(w.xyz, w.faces, w.face_rgb, camera or w.camera, settings or w.settings, params or w.params,
+                         fid, width, height, precision=precision, want=want)
+
+
+def steps_case():
+    w = wl.plain_small(96, 64)
+    w.settings.field_weight = 0.75
+    w.params = wl.fixed_steps(0.05, 80, kahan=True)
+    return w
+
+
+def ref_case():
+    return wl.reference_default(96, 64)
+
+
+def assert_exact(g, o, color_tol=1):
+    np.testing.assert_array_equal(g["hit_id"], o["hit_id"])
+    np.testing.assert_array_equal(g["steps"], o["steps"])
+    np.testing.assert_array_equal(g["mapping"].view(np.uint32), o["mapping"].view(np.uint32))
+    assert np.abs(g["color"].astype(int) - o["color"].astype(int)).max() <= color_tol
+
+
+@pytest.mark.parametrize("bvh", [False, True])
+@pytest.mark.parametrize("case", ["steps", "reference"])
+@pytest.mark.parametrize("name", EXACT_FIELDS)
+def test_precise_bit_exact(engine, oracle, name, case, bvh):
+    w = steps_case() if case == "steps" else ref_case()
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=bvh)
+    g = gpu_render(engine, w, field(engine, name, True))
+    o = oracle_render(oracle, w, _abi.FIELD_IDS[name], w.width, w.height)
+    assert_exact(g, o)
+
+
+@pytest.mark.parametrize("name", TRANSC_FIELDS)
+def test_precise_transcendental_fields_close(engine, oracle, name):
+    w = steps_case()
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    g = gpu_render(engine, w, field(engine, name, True))
+    o = oracle_render(oracle, w, _abi.FIELD_IDS[name], w.width, w.height)
+    same = g["hit_id"] == o["hit_id"]
+    assert same.mean() >= 0.99
+    np.testing.assert_array_equal(g["steps"], o["steps"])
+    d = np.abs(g["mapping"][..., :3] - o["mapping"][..., :3]).max(axis=-1)
+    tol = 1e-2 if name == "lens" else 1e-4  # lens orbits are chaotic near the origin
+    assert np.percentile(d[same], 99) <= tol
+
+
+@pytest.mark.parametrize("name", ["linear", "twist"])
+def test_fast_vs_fp64(engine, oracle, name):
+    """1080p workload shape at 1/10 size: h = 0.005, 4000 steps, Kahan sums."""
+    w = wl.frames_1080p(192, 108)
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    g = gpu_render(engine, w, field(engine, name, False))
+    o = oracle_render(oracle, w, _abi.FIELD_IDS[name], w.width, w.height, precision=64)
+    err = np.abs(g["mapping"][..., :3].astype(np.float64) - o["mapping64"][..., :3]).max(axis=-1)
+    assert err.max() <= 1e-4, err.max()
+    assert np.mean(g["hit_id"] != o["hit_id"]) <= 0.001
+    assert (g["steps"] == 4000).all()
+
+
+def test_bvh_equals_brute_force_cornell(engine):
+    w = wl.plain_small(256, 256)
+    fld = field(engine, "twist", False)
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=False)
+    a = gpu_render(engine, w, fld)
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    assert engine.scene_info()["nodes"] > 1
+    b = gpu_render(engine, w, fld)
+    for k in a:
+        np.testing.assert_array_equal(a[k], b[k])
+
+
+def test_bvh_equals_brute_force_spheres(engine):
+    xyz, faces, rgb = scene.cornell_with_spheres(seed=0)
+    assert len(faces) == 36 + 4 * 20480
+    views = wl.batch_views(3, seed=1, min_side=96, max_side=128)
+    fld = field(engine, "twist", False)
+    for W, H, camera, params, _ in views:
+        params.stop_on_hit = 1
+        w = wl.Workload("v", xyz, faces, rgb, W, H, camera, wl.settings(), params)
+        engine.upload_scene(xyz, faces, rgb, bvh=False)
+        a = gpu_render(engine, w, fld)
+        engine.upload_scene(xyz, faces, rgb, bvh=True)
+        b = gpu_render(engine, w, fld)
+        for k in a:
+            np.testing.assert_array_equal(a[k], b[k])
+
+
+@pytest.mark.parametrize("size", [(1, 1), (2, 2), (33, 17), (7, 130)])
+def test_odd_and_tiny_sizes(engine, oracle, size):
+    W, H = size
+    w = steps_case()
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    g = gpu_render(engine, w, field(engine, "linear", True), W, H)
+    o = oracle_render(oracle, w, _abi.FIELD_IDS["linear"], W, H)
+    np.testing.assert_array_equal(g["hit_id"], o["hit_id"])
+    np.testing.assert_array_equal(np.isnan(g["mapping"]), np.isnan(o["mapping"]))
+    m = ~np.isnan(o["mapping"])
+    np.testing.assert_array_equal(g["mapping"][m], o["mapping"][m])
+
+
+def test_empty_scene_and_linear_mode(engine, oracle):
+    w = steps_case()
+    engine.upload_scene(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32), None, bvh=True)
+    g = gpu_render(engine, w, field(engine, "linear", True))
+    assert (g["hit_id"] == -1).all()
+    assert (g["color"][..., :3] == 0).all() and (g["color"][..., 3] == 255).all()
+    # linear_mode (main_view.wgsl:368-370): one straight ray, max distance 100
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    p = wl.fixed_steps(0.05, 80)
+    p.linear_mode = 1
+    g = gpu_render(engine, w, field(engine, "linear", True), params=p)
+    o = oracle_render(oracle, w, _abi.FIELD_IDS["linear"], w.width, w.height, params=p)
+    np.testing.assert_array_equal(g["hit_id"], o["hit_id"])
+    assert np.abs(g["color"].astype(int) - o["color"].astype(int)).max() <= 1
+
+
+def test_render_host_matches_device(engine):
+    w = steps_case()
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    fld = field(engine, "lorenz", True)
+    d = gpu_render(engine, w, fld)
+    h = engine.render_host(fld, w.camera, w.settings, w.params, w.width, w.height)
+    for k in d:
+        np.testing.assert_array_equal(d[k], h[k])
+
+
+def test_compile_error_through_engine(engine):
+    with pytest.raises(_abi.LinonCompileError) as e:
+        engine.compile_field("return nope;")
+    assert "nope" in e.value.message
+    with pytest.raises(_abi.LinonCompileError):
+        engine.compile_field(predefined_source(0))  # Custom: empty body
+
+
+@pytest.mark.parametrize("fp64", [False, True])
+@pytest.mark.parametrize("srgb", [False, True])
+def test_overlay_matches_oracle(engine, oracle, fp64, srgb):
+    w = wl.lyapunov_1024(128, 128)
+    w.params = wl.fixed_steps(0.01, 300, kahan=True)
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    g = gpu_render(engine, w, field(engine, "lorenz_scaled", False))
+    st = wl.settings(overlay_mode=1, delta=2, scaling=50.0)
+    target = torch.empty((128, 128, 4), dtype=torch.uint8, device="cuda")
+    expo = torch.zeros((128, 128), dtype=torch.float32, device="cuda")
+    color = torch.from_numpy(g["color"]).cuda()
+    mapping = torch.from_numpy(g["mapping"]).cuda()
+    engine.overlay(st, 128, 128, color, mapping, target, expo, srgb=srgb, fp64=fp64)
+    torch.cuda.synchronize()
+    o_rgba, o_e = oracle.overlay(g["color"], g["mapping"], 128, 128, st, srgb=srgb, precision=64 if fp64 else 32)
+    e = expo.cpu().numpy()
+    np.testing.assert_allclose(e, o_e, rtol=1e-5, atol=1e-6)
+    assert np.abs(target.cpu().numpy().astype(int) - o_rgba.astype(int)).max() <= 1
+
+
+def test_ftle_matches_oracle(engine, oracle):
+    w = wl.lyapunov_1024(96, 96)
+    w.params = wl.fixed_steps(0.01, 200, kahan=True)
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    g = gpu_render(engine, w, field(engine, "lorenz_scaled", False))
+    mapping = torch.from_numpy(g["mapping"]).cuda()
+    out = torch.empty((96, 96), dtype=torch.float32, device="cuda")
+    engine.ftle(w.camera, w.params, 96, 96, mapping, 2.0, out)
+    torch.cuda.synchronize()
+    o = oracle.ftle(w.camera, w.params, 96, 96, g["mapping"], 2.0)
+    np.testing.assert_allclose(out.cpu().numpy(), o, rtol=1e-6, atol=1e-6)
+
+
+def test_capture_reference_matches_oracle(engine, oracle):
+    w = ref_case()
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    fld = field(engine, "lorenz", True)
+    out = torch.zeros((800, 8), dtype=torch.float32, device="cuda")
+    engine.capture_reference(fld, w.camera, w.settings, w.params, w.width, w.height, out)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().reshape(8, 100, 8)
+    ring = np.array([(-1, -1), (0, -1), (1, -1), (1, 0), (1, 1), (0, 1), (-1, 1), (-1, 0)], np.float32)
+    pos = (np.float32([0.5, 0.6]) + np.float32(0.01) * ring).astype(np.float32)
+    o = oracle.capture(_abi.FIELD_IDS["lorenz"], w.camera, w.settings, w.params, w.width, w.height, pos,
+                       0.001, 5000, 50, False)
+    np.testing.assert_array_equal(got[:, :, :4], o)
+    assert (got[:, :, 7] == 0.5).all()
+    np.testing.assert_array_equal(got[1, 0, 4:7], [0.5, 0.5, 0.0])
+
+
+def test_capture_paths_matches_oracle(engine, oracle):
+    w = wl.plain_small(64, 64)
+    fld = field(engine, "translation_x", True)
+    rng = np.random.default_rng(3)
+    pos = rng.uniform(0.2, 0.8, size=(37, 2)).astype(np.float32)
+    n_steps, every = 301, 7
+    npts = -(-n_steps // every) + 1
+    out = torch.zeros((37, npts, 4), dtype=torch.float32, device="cuda")
+    engine.capture_paths(fld, w.camera, w.settings, w.params, 64, 64, pos, 0.01, n_steps, every, out)
+    torch.cuda.synchronize()
+    o = oracle.capture(_abi.FIELD_IDS["translation_x"], w.camera, w.settings, w.params, 64, 64, pos, 0.01,
+                       n_steps, every, True)
+    np.testing.assert_array_equal(out.cpu().numpy(), o)
+
+
+@pytest.mark.parametrize("shape", [(64, 64), (96, 48), (1, 1), (5, 3)])
+def test_outline_select_matches_oracle(engine, oracle, shape):
+    W, H = shape
+    rng = np.random.default_rng(W * 7 + H)
+    for density in (0.0, 0.01, 0.3):
+        e = (rng.random((H, W)) < density).astype(np.float32) * rng.uniform(0.8, 2.0, size=(H, W)).astype(np.float32)
+        t = torch.from_numpy(e).cuda()
+        pix, pos = engine.outline_select(t, W, H, 0.8)
+        o = oracle.outline_select(e, W, H, 0.8)
+        np.testing.assert_array_equal(pix, o)
+
+
+def test_quantile_matches_numpy(engine):
+    rng = np.random.default_rng(5)
+    e = rng.standard_normal((200, 300)).astype(np.float32)
+    t = torch.from_numpy(e).cuda()
+    for q in (0.0, 0.5, 0.95, 1.0):
+        got = engine.exponent_quantile(t, 300, 200, q, border=3)
+        inner = np.sort(e[3:-3, 3:-3].ravel())
+        assert got == inner[int(np.floor(q * (len(inner) - 1)))]
+
+
+def batch_setup(engine, precise, n=6, seed=4):
+    xyz, faces, rgb = scene.cornell_with_spheres(seed=seed, subdivisions=2)
+    engine.upload_scene(xyz, faces, rgb, bvh=True)
+    names = ["linear", "twist", "lorenz_scaled"]
+    flds = [field(engine, nme, precise) for nme in names]
+    views, planes = [], []
+    for (W, H, camera, params, fidx) in wl.batch_views(n, seed=seed, min_side=24, max_side=90, n_fields=3):
+        params.max_steps = min(params.max_steps, 200)
+        fp = FramePlanes.allocate(W, H)
+        v = _abi.View()
+        v.camera = camera
+        v.settings = wl.settings()
+        v.params = params
+        v.width, v.height, v.field_index = W, H, fidx
+        v.out = fp.abi()
+        views.append(v)
+        planes.append(fp)
+    return flds, views, planes
+
+
+def snapshot(planes):
+    torch.cuda.synchronize()
+    return [{k: getattr(p, k).cpu().numpy().copy() for k in ("color", "mapping", "hit_id", "steps")} for p in planes]
+
+
+@pytest.mark.parametrize("precise", [True, False])
+def test_batch_equals_plain(engine, precise):
+    flds, views, planes = batch_setup(engine, precise)
+    engine.render_views_plain(flds, views)
+    a = snapshot(planes)
+    for p in planes:
+        for k in ("color", "mapping", "hit_id", "steps"):
+            getattr(p, k).zero_()
+    tuning = _abi.BatchTuning(16, 64, 0, 8, 4)
+    engine.render_batch(flds, views, tuning)
+    engine.synchronize()
+    b = snapshot(planes)
+    for x, y in zip(a, b):
+        for k in x:
+            if precise:
+                np.testing.assert_array_equal(x[k], y[k])
+            else:
+                assert np.mean(x[k] != y[k]) <= 0.001
+
+
+def test_batch_alone_equals_in_mix(engine):
+    flds, views, planes = batch_setup(engine, True, n=5)
+    engine.render_batch(flds, views[:1])
+    alone = snapshot(planes[:1])[0]
+    for p in planes:
+        p.hit_id.fill_(-7)
+    engine.render_batch(flds, views)
+    engine.synchronize()
+    mixed = snapshot(planes[:1])[0]
+    for k in alone:
+        np.testing.assert_array_equal(alone[k], mixed[k])
+
+
+def test_batch_graph_replay_and_tuning(engine):
+    flds, views, planes = batch_setup(engine, False, n=4)
+    engine.render_batch(flds, views)
+    first = snapshot(planes)
+    engine.render_batch(flds, views)  # replays the captured graph
+    second = snapshot(planes)
+    for x, y in zip(first, second):
+        for k in x:
+            np.testing.assert_array_equal(x[k], y[k])
+    t, ms = engine.autotune_batch(flds, views)
+    assert t.quantum in (8, 16, 32, 64) and ms > 0
+
+
+def test_hbm_budget_admission():
+    from linon_gb300 import Engine
+    e = Engine(0, hbm_budget=1 << 20)
+    try:
+        xyz, faces, rgb = scene.cornell_with_spheres(seed=0)
+        with pytest.raises(_abi.LinonError) as err:
+            e.upload_scene(xyz, faces, rgb)
+        assert err.value.status == _abi.LINON_ENOMEM
+        e.upload_scene(*scene.cornell_unit())
+    finally:
+        e.close()
+
+
+def test_main_view_mirror(engine):
+    from linon_gb300.main_view import MainView
+    xyz, faces, _, center = scene.cornell_reference()
+    mv = MainView(engine, xyz, faces, center, 64, 48)
+    mv.render()
+    mv.reload_shader(None, predefined_source(_abi.FIELD_IDS["rotation"]))
+    with pytest.raises(_abi.LinonCompileError):
+        mv.reload_shader(None, "return undefined;")
+    mv.render_high_accuracy(mv.field_function)
+    pos = mv.render_outline_rays(mv.field_function)
+    torch.cuda.synchronize()
+    assert pos.shape == (8, 2)
+    assert mv.texture.shape == (48, 64, 4)
