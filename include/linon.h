@@ -205,6 +205,12 @@ int linon_wgsl_translate(const char* field_body, const char* helpers_src,
 int linon_render(linon_ctx* ctx, const linon_field* field,
                  const linon_camera* camera, const linon_settings* settings,
                  const linon_march_params* params, const linon_frame* out);
+/* Evaluates the field at n points: in = n x 13 floats (p_prev.xyz, p.xyz,
+ * v0.xyz, v.xyz, t), out = n x 3 floats; both device pointers.  This is the
+ * field_function of main_view.wgsl:148 called on its own (field probes,
+ * glyph visualisation).                                                    */
+int linon_field_eval(linon_ctx* ctx, const linon_field* field, const float* in,
+                     float* out, int64_t n);
 /* Same, with host output buffers (copied back; NULL planes are skipped).  */
 int linon_render_host(linon_ctx* ctx, const linon_field* field,
                       const linon_camera* camera, const linon_settings* settings,

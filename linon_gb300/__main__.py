@@ -1,0 +1,111 @@
+"""Command line: render one workload with the engine.
+
+    python -m linon_gb300 render --workload frames_1080p --field twist \
+        --width 480 --height 270 --repeat 2 [--precise] [--brute-force]
+    python -m linon_gb300 batch --views 64 --repeat 2 [--plain]
+    python -m linon_gb300 validate --field lens        # NVRTC report, no GPU
+
+Prints one JSON line with the device time per launch (CUDA events).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import statistics
+
+from . import _abi, workloads as wl
+from .engine import Engine, FramePlanes, predefined_source, validate_field
+
+
+def _field_id(name):
+    return _abi.FIELD_IDS[name]
+
+
+def cmd_render(a):
+    import torch
+    w = getattr(wl, a.workload)(a.width, a.height)
+    eng = Engine(0)
+    eng.set_stream(torch.cuda.current_stream())
+    eng.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=not a.brute_force)
+    fld = eng.compile_field(predefined_source(_field_id(a.field)), precise=a.precise)
+    planes = FramePlanes.allocate(w.width, w.height)
+    ts = []
+    for _ in range(a.repeat):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        eng.render(fld, w.camera, w.settings, w.params, planes)
+        e.record()
+        eng.synchronize()
+        e.synchronize()
+        ts.append(s.elapsed_time(e))
+    steps = int(planes.steps.sum().item())
+    hits = float((planes.hit_id >= 0).float().mean().item())
+    print(json.dumps({"workload": w.name, "field": a.field, "width": w.width, "height": w.height,
+                      "ms": ts, "ray_steps": steps, "ray_steps_per_s": steps / (statistics.median(ts) * 1e-3),
+                      "hit_fraction": hits}))
+    eng.close()
+
+
+def cmd_batch(a):
+    import torch
+    w = wl.batch_uneven(a.views, seed=a.seed)
+    eng = Engine(0)
+    eng.set_stream(torch.cuda.current_stream())
+    eng.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    flds = [eng.compile_field(predefined_source(fid)) for fid in w.fields]
+    views, planes = [], []
+    for (W, H, camera, params, fidx) in w.extra["views"]:
+        p = FramePlanes.allocate(W, H)
+        v = _abi.View()
+        v.camera, v.settings, v.params = camera, wl.settings(), params
+        v.width, v.height, v.field_index = W, H, fidx
+        v.out = p.abi()
+        views.append(v)
+        planes.append(p)
+    ts = []
+    for _ in range(a.repeat):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        if a.plain:
+            eng.render_views_plain(flds, views)
+        else:
+            eng.render_batch(flds, views)
+        e.record()
+        eng.synchronize()
+        e.synchronize()
+        ts.append(s.elapsed_time(e))
+    steps = sum(int(p.steps.sum().item()) for p in planes)
+    print(json.dumps({"views": len(views), "plain": a.plain, "ms": ts, "ray_steps": steps,
+                      "ray_steps_per_s": steps / (statistics.median(ts) * 1e-3)}))
+    eng.close()
+
+
+def cmd_validate(a):
+    print(validate_field(predefined_source(_field_id(a.field)), precise=a.precise))
+
+
+def main():
+    ap = argparse.ArgumentParser(prog="python -m linon_gb300")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    r = sub.add_parser("render")
+    r.add_argument("--workload", default="frames_1080p")
+    r.add_argument("--field", default="twist")
+    r.add_argument("--width", type=int, default=480)
+    r.add_argument("--height", type=int, default=270)
+    r.add_argument("--repeat", type=int, default=2)
+    r.add_argument("--precise", action="store_true")
+    r.add_argument("--brute-force", action="store_true")
+    b = sub.add_parser("batch")
+    b.add_argument("--views", type=int, default=64)
+    b.add_argument("--seed", type=int, default=0)
+    b.add_argument("--repeat", type=int, default=2)
+    b.add_argument("--plain", action="store_true")
+    v = sub.add_parser("validate")
+    v.add_argument("--field", default="twist")
+    v.add_argument("--precise", action="store_true")
+    a = ap.parse_args()
+    {"render": cmd_render, "batch": cmd_batch, "validate": cmd_validate}[a.cmd](a)
+
+
+if __name__ == "__main__":
+    main()

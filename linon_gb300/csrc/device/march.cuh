@@ -143,6 +143,57 @@ __device__ __forceinline__ HitRec intersect_segment(const SceneView& sc, const v
   return best;
 }
 
+// Lower bound on the distance from q to any triangle of the scene: the
+// distance to the nearest (inflated) leaf box, found by a pruned traversal
+// that visits the nearer child first.  A segment starting at q and shorter
+// than this bound cannot reach any inflated box, so it cannot hit anything
+// the brute-force loop would hit (the same margin argument as the culling).
+__device__ __forceinline__ float box_dist2(const float4& lo, const float4& hi, const vec3f& q) {
+  const float dx = fmaxf(fmaxf(lo.x - q.x, q.x - hi.x), 0.0f);
+  const float dy = fmaxf(fmaxf(lo.y - q.y, q.y - hi.y), 0.0f);
+  const float dz = fmaxf(fmaxf(lo.z - q.z, q.z - hi.z), 0.0f);
+  return dx * dx + dy * dy + dz * dz;
+}
+
+__device__ __forceinline__ float nearest_leaf_bound(const SceneView& sc, const vec3f& q) {
+  float best = 3.0e38f;  // squared distance
+  int stack[LINON_BVH_STACK];
+  int sp = 0;
+  int node = 0;
+  float nd = box_dist2(sc.nodes[0], sc.nodes[1], q);
+  for (;;) {
+    if (nd < best) {
+      const float4 lo = sc.nodes[2 * node];
+      const float4 hi = sc.nodes[2 * node + 1];
+      const int count = __float_as_int(hi.w);
+      if (count > 0) {
+        best = nd;
+      } else {
+        const int first = __float_as_int(lo.w);
+        const float d0 = box_dist2(sc.nodes[2 * first], sc.nodes[2 * first + 1], q);
+        const float d1 = box_dist2(sc.nodes[2 * first + 2], sc.nodes[2 * first + 3], q);
+        const int near = d0 <= d1 ? first : first + 1;
+        const float dnear = fminf(d0, d1), dfar = fmaxf(d0, d1);
+        if (dfar < best) {
+          // the far child is revisited with its distance re-derived on pop;
+          // the tree depth is capped below the stack size, and a full stack
+          // would end the query with the trivial bound 0 (no skipping)
+          if (sp >= LINON_BVH_STACK) return 0.0f;
+          stack[sp++] = near == first ? first + 1 : first;
+        }
+        node = near;
+        nd = dnear;
+        continue;
+      }
+    }
+    if (sp == 0) break;
+    node = stack[--sp];
+    nd = box_dist2(sc.nodes[2 * node], sc.nodes[2 * node + 1], q);
+  }
+  // shrink by a relative 1e-5 against rounding of the distance itself
+  return best >= 3.0e38f ? 3.0e38f : sqrtf(best) * 0.99999f;
+}
+
 // Shading of ray_color, main_view.wgsl:199-217 (camera is the light source).
 __device__ __forceinline__ wgsl::vec4f shade_hit(const SceneView& sc, const HitRec& hit,
                                                  const vec3f& direction) {
@@ -218,8 +269,10 @@ struct RayState {
   float t, ct;          // time and its Kahan carry
   float h, last_diff;
   wgsl::vec4f color;
+  float safe;           // distance the ray may travel before it must be tested again
   int face;
   int steps;
+  int cool;             // steps left before the next safe-distance query
   bool has_color;
 };
 
@@ -237,6 +290,8 @@ __device__ __forceinline__ void ray_init(RayState& r, const vec3f& origin, const
   r.color = wgsl::vec4f(0.0f, 0.0f, 0.0f, 0.0f);
   r.face = -1;
   r.steps = 0;
+  r.safe = 0.0f;
+  r.cool = 0;
   r.has_color = false;
 }
 
@@ -279,17 +334,37 @@ __device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevM
   r.dir = (1.0f - w) * r.dir + w * v;
   const vec3f step_dir = r.dir * h;
   if (!r.has_color) {
-    const float len = wgsl::length(step_dir);
+    // Safe-distance skip (BVH scenes): the L1 length bounds the segment's
+    // Euclidean length, so a segment within the remaining safe distance of
+    // its start cannot reach any leaf box and needs no test.
+    const float reach = fabsf(step_dir.x) + fabsf(step_dir.y) + fabsf(step_dir.z);
+    if (sc.n_nodes > 0 && reach <= r.safe) {
+      r.safe -= reach;
+    } else {
+      const float len = wgsl::length(step_dir);
 #if defined(LINON_PRECISE)
-    const vec3f dirn = step_dir / len;
+      const vec3f dirn = step_dir / len;
 #else
-    const vec3f dirn = wgsl::normalize(step_dir);
+      const vec3f dirn = wgsl::normalize(step_dir);
 #endif
-    HitRec hit = intersect_segment(sc, r.p, dirn, len, r.p + step_dir, err);
-    if (hit.t > 0.0f && hit.t < len) {
-      r.color = shade_hit(sc, hit, dirn);
-      r.has_color = r.color.w > 0.0f;
-      if (r.has_color) r.face = hit.id;
+      const vec3f seg_end = r.p + step_dir;
+      HitRec hit = intersect_segment(sc, r.p, dirn, len, seg_end, err);
+      if (hit.t > 0.0f && hit.t < len) {
+        r.color = shade_hit(sc, hit, dirn);
+        r.has_color = r.color.w > 0.0f;
+        if (r.has_color) r.face = hit.id;
+      }
+      r.safe = 0.0f;
+      if (!r.has_color && sc.n_nodes > 0) {
+        if (r.cool > 0) {
+          r.cool--;
+        } else {
+          // bound from the segment's end, where the next segment starts
+          r.safe = nearest_leaf_bound(sc, seg_end);
+          // close to geometry the bound buys little: test plainly for a while
+          if (r.safe < 4.0f * reach) r.cool = 8;
+        }
+      }
     }
   }
   if (KAHAN) {

@@ -61,6 +61,82 @@ WG_HD unsigned to_u32(float x) {
 WG_HD unsigned to_u32(int x) { return unsigned(x); }
 WG_HD unsigned to_u32(unsigned x) { return x; }
 
+// Sine and cosine of one argument with one range reduction (fast modules).
+// Method: Cody & Waite's additive reduction x = q * pi/2 + r with pi/2 split
+// into three floats (each product applied by an FMA), then the Taylor series
+// of sin to r^9 and of cos to r^10 on |r| <= pi/4 (truncation below 2.5e-9
+// relative, under half an FP32 ulp), and the quadrant's swap and signs.
+// |x| >= 65536 (and inf/NaN) take the CUDA library's sincosf.
+WG_HD void sincos_fast(float x, float* s, float* c) {
+#if defined(__CUDA_ARCH__)
+  if (!(fabsf(x) < 65536.0f)) {
+    sincosf(x, s, c);
+    return;
+  }
+  const float q = rintf(x * 0x1.45f306p-1f);  // x * 2/pi
+  float r = fmaf(-q, 0x1.921fb6p+0f, x);      // pi/2 = P1 + P2 + P3
+  r = fmaf(-q, -0x1.777a5cp-25f, r);
+  r = fmaf(-q, -0x1.ee59dap-50f, r);
+  const float r2 = r * r;
+  float ps = fmaf(r2, 2.75573192e-6f, -1.98412698e-4f);  // 1/9!, -1/7!
+  ps = fmaf(r2, ps, 8.33333333e-3f);                       // 1/5!
+  ps = fmaf(r2, ps, -1.66666667e-1f);                      // -1/3!
+  const float sn = fmaf(r * r2, ps, r);
+  float pc = fmaf(r2, -2.75573192e-7f, 2.48015873e-5f);   // -1/10!, 1/8!
+  pc = fmaf(r2, pc, -1.38888889e-3f);                      // -1/6!
+  pc = fmaf(r2, pc, 4.16666667e-2f);                       // 1/4!
+  pc = fmaf(r2, pc, -0.5f);                                // -1/2!
+  const float cs = fmaf(r2, pc, 1.0f);
+  const int qi = int(q) & 3;
+  const float a = (qi & 1) ? cs : sn;
+  const float b = (qi & 1) ? sn : cs;
+  *s = (qi & 2) ? -a : a;
+  *c = ((qi + 1) & 2) ? -b : b;
+#else
+  *s = sinf(x);
+  *c = cosf(x);
+#endif
+}
+
+// sin/cos for the helpers: the shared reduction in fast modules, the CUDA
+// library functions in precise modules (as the restatement uses its libm).
+WG_HD void sincos_(float x, float* s, float* c) {
+#if defined(LINON_PRECISE) || !defined(__CUDA_ARCH__)
+  *s = sinf(x);
+  *c = cosf(x);
+#else
+  sincos_fast(x, s, c);
+#endif
+}
+
+WG_HD float sin_(float x) {
+  float s, c;
+  sincos_(x, &s, &c);
+  return s;
+}
+WG_HD float cos_(float x) {
+  float s, c;
+  sincos_(x, &s, &c);
+  return c;
+}
+
+// pow with an exponent known at the call site (the front end emits this for
+// constant exponents).  Fast modules evaluate the common rational exponents
+// with sqrt and products; precise modules keep powf.
+WG_HD float pow_k(float x, float k) {
+#if !defined(LINON_PRECISE) && defined(__CUDA_ARCH__)
+  if (k == 1.0f) return x;
+  if (k == 2.0f) return x * x;
+  if (k == 3.0f) return x * x * x;
+  if (k == 4.0f) { const float y = x * x; return y * y; }
+  if (k == 0.5f) return sqrtf(x);
+  if (k == 1.5f) return x * sqrtf(x);
+  if (k == -0.5f) return rsqrtf(x);
+  if (k == -1.0f) return 1.0f / x;
+#endif
+  return powf(x, k);
+}
+
 // ---------------------------------------------------------------------------
 // vectors
 // ---------------------------------------------------------------------------
@@ -149,6 +225,16 @@ WG_VEC_BINOP(-)
 WG_VEC_BINOP(*)
 WG_VEC_BINOP(/)
 #undef WG_VEC_BINOP
+
+#if !defined(LINON_PRECISE) && defined(__CUDA_ARCH__)
+// Fast modules divide a float vector by a scalar with one reciprocal.
+template <int N> WG_HD vec<float, N> operator/(const vec<float, N>& a, float s) {
+  const float r = 1.0f / s;
+  vec<float, N> o;
+  for (int i = 0; i < N; ++i) o[i] = a[i] * r;
+  return o;
+}
+#endif
 
 template <class T, int N> WG_HD vec<T, N> operator-(const vec<T, N>& a) {
   vec<T, N> r;
@@ -284,8 +370,8 @@ WG_HD float determinant(const mat<3, 3>& m) {
     for (int i = 0; i < N; ++i) r[i] = NAME(v[i]);                                 \
     return r;                                                                      \
   }
-WG_UNARY(sin, sinf(x))
-WG_UNARY(cos, cosf(x))
+WG_UNARY(sin, sin_(x))
+WG_UNARY(cos, cos_(x))
 WG_UNARY(tan, tanf(x))
 WG_UNARY(asin, asinf(x))
 WG_UNARY(acos, acosf(x))
@@ -452,15 +538,18 @@ template <int N> WG_HD bool any(const vec<bool, N>& v) {
 #define LINON_PI 3.14159265358979323846f
 
 WG_HD vec3f rotateX(const vec3f& v, float phi) {  // main_view.wgsl:78-84
-  float c = cosf(phi), s = sinf(phi);
+  float s, c;
+  sincos_(phi, &s, &c);
   return make_mat(vec3f(1.0f, 0.0f, 0.0f), vec3f(0.0f, c, s), vec3f(0.0f, -s, c)) * v;
 }
 WG_HD vec3f rotateY(const vec3f& v, float phi) {  // main_view.wgsl:86-92
-  float c = cosf(phi), s = sinf(phi);
+  float s, c;
+  sincos_(phi, &s, &c);
   return make_mat(vec3f(c, 0.0f, -s), vec3f(0.0f, 1.0f, 0.0f), vec3f(s, 0.0f, c)) * v;
 }
 WG_HD vec3f rotateZ(const vec3f& v, float phi) {  // main_view.wgsl:94-100: third column zero
-  float c = cosf(phi), s = sinf(phi);
+  float s, c;
+  sincos_(phi, &s, &c);
   return make_mat(vec3f(c, s, 0.0f), vec3f(-s, c, 0.0f), vec3f(0.0f, 0.0f, 0.0f)) * v;
 }
 WG_HD vec3f translate(const vec3f& v, float dx, float dy, float dz) {  // main_view.wgsl:102-108

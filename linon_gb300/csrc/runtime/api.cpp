@@ -528,6 +528,21 @@ int linon_render(linon_ctx* ctx, const linon_field* field, const linon_camera* c
   LINON_TRY_END
 }
 
+int linon_field_eval(linon_ctx* ctx, const linon_field* field, const float* in, float* out, int64_t n) {
+  LINON_TRY_BEGIN
+  if (int st = enter(ctx)) return st;
+  if (int st = field_valid(ctx, field)) return st;
+  if (n < 0 || n > (int64_t(1) << 31) - 1) return set_error(LINON_EINVAL, "n out of range");
+  if (n == 0) return LINON_OK;
+  if (!in || !out) return set_error(LINON_EINVAL, "null field_eval buffers");
+  cudaKernel_t k = field->mod->kernels.at("linon_field_eval");
+  int nn = int(n);
+  void* args[] = {&in, &out, &nn};
+  LINON_CUDA(cudaLaunchKernel((const void*)k, dim3(unsigned((n + 255) / 256)), dim3(256), args, 0, ctx->stream));
+  return LINON_OK;
+  LINON_TRY_END
+}
+
 int linon_render_host(linon_ctx* ctx, const linon_field* field, const linon_camera* camera,
                       const linon_settings* settings, const linon_march_params* params,
                       int32_t width, int32_t height, uint8_t* color, float* mapping, int32_t* hit_id,

@@ -1542,7 +1542,10 @@ class Compiler {
     }
     if (n == "pow" || n == "atan2" || n == "step") {
       need_args(e, 2);
-      return componentwise(unify_args(e, 0, 2, true, false), 0, n == "step" ? 0 : 1);
+      componentwise(unify_args(e, 0, 2, true, false), 0, n == "step" ? 0 : 1);
+      // a constant scalar exponent lets fast modules use sqrt / products
+      if (n == "pow" && !e.cst && e.ty.cat == Ty::Scalar && e.args[1]->cst) callinfo[&e].fn = "::wgsl::pow_k";
+      return;
     }
     if (n == "min" || n == "max") {
       need_args(e, 2);

@@ -141,6 +141,14 @@ class Engine:
         check(self.lib.linon_render(self.ctx, field.handle, C.byref(camera), C.byref(settings),
                                     C.byref(params), C.byref(f)))
 
+    def field_eval(self, field: Field, inputs):
+        """Evaluates the field at n points (torch CUDA tensor [n, 13]) -> [n, 3]."""
+        import torch
+        x = inputs.contiguous().to(torch.float32)
+        out = torch.empty((x.shape[0], 3), dtype=torch.float32, device=x.device)
+        check(self.lib.linon_field_eval(self.ctx, field.handle, x.data_ptr(), out.data_ptr(), x.shape[0]))
+        return out
+
     def render_host(self, field: Field, camera, settings, params, width: int, height: int,
                     color=True, mapping=True, hit_id=True, steps=True):
         """Renders into host numpy arrays (copies inside the call)."""

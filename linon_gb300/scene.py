@@ -126,6 +126,24 @@ def icosphere(subdivisions: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)):
     return xyz.astype(np.float32), np.asarray(faces, dtype=np.uint32)
 
 
+def coplanar_groups(xyz, faces, tol: float = 1e-5) -> np.ndarray:
+    """Group id per face; faces lying in one plane share an id.  Hits on
+    coplanar, overlapping faces (the Cornell light panel in the ceiling, the
+    block footprints in the floor) are decided by rounding ties, so accuracy
+    checks count a hit-id difference inside one group as a tie."""
+    v = np.asarray(xyz, np.float64)[np.asarray(faces, np.int64)]
+    n = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
+    ln = np.linalg.norm(n, axis=1, keepdims=True)
+    n = np.where(ln > 0, n / np.where(ln > 0, ln, 1), 0)
+    # canonical orientation: first non-zero component positive
+    sign = np.sign(n[np.arange(len(n)), np.argmax(np.abs(n) > tol, axis=1)])
+    n = n * np.where(sign == 0, 1, sign)[:, None]
+    d = np.einsum("ij,ij->i", n, v[:, 0])
+    key = np.round(np.concatenate([n, d[:, None]], axis=1) / tol).astype(np.int64)
+    _, ids = np.unique(key, axis=0, return_inverse=True)
+    return ids.ravel()
+
+
 def merge(*meshes):
     """Concatenates (xyz, faces[, rgb]) meshes; faces are re-indexed."""
     xs, fs, cs = [], [], []

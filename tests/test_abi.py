@@ -1,0 +1,81 @@
+"""The C ABI library: loads without a GPU, exports every declared symbol,
+data layouts match the reference's uniforms, host-only entry points work."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from linon_gb300 import _abi, outline_indices
+from linon_gb300.engine import predefined_name, predefined_source
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "linon.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(linon_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_functions()
+    assert len(names) >= 30
+    for n in names:
+        assert hasattr(lib, n), n
+    # and every declared symbol has a ctypes prototype
+    assert set(names) == set(_abi.PROTOTYPES), set(names) ^ set(_abi.PROTOTYPES)
+
+
+def test_struct_layouts():
+    assert C.sizeof(_abi.Camera) == 112       # CameraUniform, main_view.rs:12-19
+    assert C.sizeof(_abi.Settings) == 24      # Settings, main_view.rs:43-51
+    assert C.sizeof(_abi.RaySample) == 32     # RaySample, main_view.wgsl:55-58
+    assert _abi.Settings.lyapunov_scaling.offset == 20
+    assert _abi.Camera.view_matrix.offset == 48
+
+
+def test_reference_params(lib):
+    p = _abi.reference_params()
+    assert (p.h_initial, p.t_max, p.max_steps, p.adaptive) == (pytest.approx(0.1), 5.0, 0, 1)
+    assert (p.h_fine, p.h_fine_above) == (pytest.approx(0.001), pytest.approx(0.002))
+    assert (p.focal_length, p.viewport_height) == (pytest.approx(0.035), pytest.approx(0.025))
+
+
+def test_status_strings_and_predefined(lib):
+    assert lib.linon_abi_version() == 1
+    assert lib.linon_status_string(_abi.LINON_ECOMPILE) == b"field function compilation failed"
+    assert predefined_name(3) == "Mirage (spherical sigmoid)"
+    assert predefined_name(9) == "Roessler attractor"
+    assert predefined_source(7) == "return normalize(v0 + rotateZ(v0, PI * t));"
+    assert lib.linon_predefined_source(99) is None
+
+
+def test_outline_indices_restated():
+    """src/ray_samples.rs:29-49 restated in numpy: 4 sides x 99 quads x 4 tris."""
+    idx = outline_indices()
+    assert idx.shape == (4 * 99 * 4, 3)
+    exp = []
+    for a, b, c in ((0, 1, 2), (2, 3, 4), (4, 5, 6), (6, 7, 0)):
+        for i in range(99):
+            A, B, Cc = a * 100 + i, b * 100 + i, c * 100 + i
+            exp += [(A, B + 1, A + 1), (A, B, B + 1), (B, Cc, B + 1), (Cc, Cc + 1, B + 1)]
+    np.testing.assert_array_equal(idx, np.array(exp, np.uint16))
+
+
+def test_create_without_gpu_fails_cleanly(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    ctx = C.c_void_p()
+    st = lib.linon_create(0, 0, C.byref(ctx))
+    assert st in (_abi.LINON_ECUDA, _abi.LINON_EINVAL)
+    assert ctx.value is None
+    assert lib.linon_last_error()
+
+
+def test_null_arguments_rejected(lib):
+    assert lib.linon_render(None, None, None, None, None, None) == _abi.LINON_EINVAL
+    assert lib.linon_scene_upload(None, None, 0, None, 0, None, 0) == _abi.LINON_EINVAL
+    assert lib.linon_destroy(None) == _abi.LINON_OK

@@ -91,17 +91,54 @@ def test_precise_transcendental_fields_close(engine, oracle, name):
     assert np.percentile(d[same], 99) <= tol
 
 
-@pytest.mark.parametrize("name", ["linear", "twist"])
-def test_fast_vs_fp64(engine, oracle, name):
-    """1080p workload shape at 1/10 size: h = 0.005, 4000 steps, Kahan sums."""
-    w = wl.frames_1080p(192, 108)
+@pytest.mark.parametrize("name", ["linear", "twist", "lens"])
+def test_fast_vs_fp64_1080p(engine, oracle, name):
+    """The 1080p workload (h = 0.005, 4000 steps, Kahan sums), fast module,
+    full frame on the GPU, 4000 random pixels against the FP64 oracle.
+    Bars: endpoint error <= 1e-4 scene units on smooth fields; hit-id
+    mismatch <= 0.1% excluding coplanar ties (light panel / ceiling, block
+    footprints / floor: which of two coplanar faces a ray meets is a rounding
+    tie).  The lens field's rays are captured into orbits around the origin,
+    a chaotic region where FP32 and FP64 separate; its error is recorded, not
+    bounded at 1e-4."""
+    w = wl.frames_1080p()
     engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
     g = gpu_render(engine, w, field(engine, name, False))
-    o = oracle_render(oracle, w, _abi.FIELD_IDS[name], w.width, w.height, precision=64)
-    err = np.abs(g["mapping"][..., :3].astype(np.float64) - o["mapping64"][..., :3]).max(axis=-1)
-    assert err.max() <= 1e-4, err.max()
-    assert np.mean(g["hit_id"] != o["hit_id"]) <= 0.001
+    rng = np.random.default_rng(11)
+    pix = np.sort(rng.choice(w.width * w.height, 4000, replace=False)).astype(np.int32)
+    o = oracle.render(w.xyz, w.faces, w.face_rgb, w.camera, w.settings, w.params, _abi.FIELD_IDS[name], w.width,
+                      w.height, pixels=pix, precision=64, want=("mapping64", "hit_id", "steps"))
+    gm = g["mapping"].reshape(-1, 4)[pix, :3].astype(np.float64)
+    gh = g["hit_id"].ravel()[pix]
+    err = np.abs(gm - o["mapping64"][:, :3]).max(axis=-1)
+    groups = scene.coplanar_groups(w.xyz, w.faces)
+    diff = gh != o["hit_id"]
+    tie = diff & (gh >= 0) & (o["hit_id"] >= 0)
+    tie[tie] = groups[gh[tie]] == groups[o["hit_id"][tie]]
+    assert np.mean(diff & ~tie) <= 0.001
     assert (g["steps"] == 4000).all()
+    if name == "lens":
+        assert np.percentile(err, 50) < 0.05
+    else:
+        assert err.max() <= 1e-4, err.max()
+
+
+def test_fast_math_accuracy(engine):
+    """Fast modules' sin/cos (one Cody-Waite reduction + Taylor polynomials)
+    and constant-exponent pow against FP64."""
+    body = "return vec3<f32>(sin(t), cos(t), pow(p.x, 1.5));"
+    fld = engine.compile_field(body)
+    n = 1 << 18
+    rng = np.random.default_rng(2)
+    x = np.zeros((n, 13), np.float32)
+    x[:, 12] = np.concatenate([rng.uniform(-4, 4, n // 2), rng.uniform(-3000, 3000, n // 2)]).astype(np.float32)
+    x[:, 3] = rng.uniform(0, 50, n).astype(np.float32)
+    out = engine.field_eval(fld, torch.from_numpy(x).cuda()).cpu().numpy().astype(np.float64)
+    t = x[:, 12].astype(np.float64)
+    assert np.abs(out[:, 0] - np.sin(t)).max() <= 2.5e-7
+    assert np.abs(out[:, 1] - np.cos(t)).max() <= 2.5e-7
+    ref = x[:, 3].astype(np.float64) ** 1.5
+    assert (np.abs(out[:, 2] - ref) / np.maximum(ref, 1e-30)).max() <= 3.6e-7
 
 
 def test_bvh_equals_brute_force_cornell(engine):
