@@ -25,16 +25,18 @@ def cmd_render(a):
     import torch
     w = getattr(wl, a.workload)(a.width, a.height)
     eng = Engine(0)
-    eng.set_stream(torch.cuda.current_stream())
+    stream = torch.cuda.Stream()
+    eng.set_stream(stream)
     eng.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=not a.brute_force)
     fld = eng.compile_field(predefined_source(_field_id(a.field)), precise=a.precise)
     planes = FramePlanes.allocate(w.width, w.height)
+    torch.cuda.synchronize()
     ts = []
     for _ in range(a.repeat):
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record()
+        s.record(stream)
         eng.render(fld, w.camera, w.settings, w.params, planes)
-        e.record()
+        e.record(stream)
         eng.synchronize()
         e.synchronize()
         ts.append(s.elapsed_time(e))
@@ -50,7 +52,8 @@ def cmd_batch(a):
     import torch
     w = wl.batch_uneven(a.views, seed=a.seed)
     eng = Engine(0)
-    eng.set_stream(torch.cuda.current_stream())
+    stream = torch.cuda.Stream()
+    eng.set_stream(stream)
     eng.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
     flds = [eng.compile_field(predefined_source(fid)) for fid in w.fields]
     views, planes = [], []
@@ -62,15 +65,16 @@ def cmd_batch(a):
         v.out = p.abi()
         views.append(v)
         planes.append(p)
+    torch.cuda.synchronize()
     ts = []
     for _ in range(a.repeat):
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record()
+        s.record(stream)
         if a.plain:
             eng.render_views_plain(flds, views)
         else:
             eng.render_batch(flds, views)
-        e.record()
+        e.record(stream)
         eng.synchronize()
         e.synchronize()
         ts.append(s.elapsed_time(e))

@@ -494,14 +494,17 @@ __device__ __forceinline__ void march_plain_kernel(const F& field, const MarchAr
   const int lx = threadIdx.x % a.tile_w, ly = threadIdx.x / a.tile_w;
   const int x = blockIdx.x * a.tile_w + lx;
   const int row = blockIdx.y * a.tile_h + ly;
-  if (x >= W || row >= H) return;
+  // Threads outside the image stay in the warp as idle lanes (no early
+  // exit) so that the per-step warp vote below always names all 32 lanes.
+  const bool in_image = x < W && row < H;
   const int gy = H - 1 - row;
   const Basis b = make_basis(a.cam, W, H, a.m.focal_length, a.m.viewport_height);
-  const vec3f dir = primary_dir(b, x, gy);
-  const size_t idx = size_t(row) * W + x;
+  const vec3f dir = primary_dir(b, in_image ? x : 0, in_image ? gy : 0);
+  const size_t idx = in_image ? size_t(row) * W + x : 0;
   RayState r;
   ray_init(r, b.origin, dir, a.m.h_initial);
   if (a.m.linear_mode) {  // main_view.wgsl:368-370
+    if (!in_image) return;
     HitRec hit = intersect_segment(sc, b.origin, dir, 100.0f, b.origin + 100.0f * dir, a.err);
     wgsl::vec4f c(0.0f, 0.0f, 0.0f, 0.0f);
     if (hit.t > 0.0f && hit.t < 100.0f) c = shade_hit(sc, hit, dir);
@@ -515,8 +518,17 @@ __device__ __forceinline__ void march_plain_kernel(const F& field, const MarchAr
     if (a.frame.steps) a.frame.steps[idx] = 0;
     return;
   }
-  while (ray_active(r, a.m)) ray_step<ADAPTIVE, KAHAN>(r, field, a.m, sc, a.err);
-  ray_store(r, a.frame, idx);
+  // The vote at the top of every step reconverges the warp: without it the
+  // lanes that diverged at a (rare) intersection test would walk the rest of
+  // the march separately, a few lanes per issued instruction.
+  bool active = in_image && ray_active(r, a.m);
+  while (__any_sync(0xffffffffu, active)) {
+    if (active) {
+      ray_step<ADAPTIVE, KAHAN>(r, field, a.m, sc, a.err);
+      active = ray_active(r, a.m);
+    }
+  }
+  if (in_image) ray_store(r, a.frame, idx);
 }
 
 // --------------------------------------------------------------------------
@@ -628,17 +640,16 @@ __device__ __forceinline__ void march_batch_kernel(const Fields& fields, const B
       if (drained) break;
       continue;
     }
-    // ---- march a quantum ----
-    if (active) {
-      const FieldRef<Fields> field{fields, fidx};
-      for (int q = 0; q < a.quantum; ++q) {
-        if (!ray_active(r, m)) break;
-        ray_step_rt(r, field, m, sc, a.err);
-      }
-      if (!ray_active(r, m)) {
-        ray_store(r, out, pix);
-        active = false;
-      }
+    // ---- march a quantum (one warp vote per step keeps the lanes converged) ----
+    const FieldRef<Fields> field{fields, fidx};
+    for (int q = 0; q < a.quantum; ++q) {
+      const bool go = active && ray_active(r, m);
+      if (!__any_sync(FULL, go)) break;
+      if (go) ray_step_rt(r, field, m, sc, a.err);
+    }
+    if (active && !ray_active(r, m)) {
+      ray_store(r, out, pix);
+      active = false;
     }
   }
 }

@@ -156,16 +156,16 @@ struct LinonField {
     return linon_user::field_function(pp, p, v0, v, t);
   }
 };
-extern "C" __global__ void __launch_bounds__(256) linon_march_a0_k0(linon::MarchArgs a) {
+extern "C" __global__ void __launch_bounds__(128) linon_march_a0_k0(linon::MarchArgs a) {
   linon::march_plain_kernel<false, false>(LinonField(), a);
 }
-extern "C" __global__ void __launch_bounds__(256) linon_march_a0_k1(linon::MarchArgs a) {
+extern "C" __global__ void __launch_bounds__(128) linon_march_a0_k1(linon::MarchArgs a) {
   linon::march_plain_kernel<false, true>(LinonField(), a);
 }
-extern "C" __global__ void __launch_bounds__(256) linon_march_a1_k0(linon::MarchArgs a) {
+extern "C" __global__ void __launch_bounds__(128) linon_march_a1_k0(linon::MarchArgs a) {
   linon::march_plain_kernel<true, false>(LinonField(), a);
 }
-extern "C" __global__ void __launch_bounds__(256) linon_march_a1_k1(linon::MarchArgs a) {
+extern "C" __global__ void __launch_bounds__(128) linon_march_a1_k1(linon::MarchArgs a) {
   linon::march_plain_kernel<true, true>(LinonField(), a);
 }
 extern "C" __global__ void __launch_bounds__(256) linon_capture(linon::CaptureArgs a) {
