@@ -42,6 +42,7 @@ struct SceneView {
   const float4* face_rgb;
   int n_tris;
   int n_nodes;
+  float margin;
 };
 
 __device__ __forceinline__ vec3f xyz(const float4& a) { return vec3f(a.x, a.y, a.z); }
@@ -155,7 +156,24 @@ __device__ __forceinline__ float box_dist2(const float4& lo, const float4& hi, c
   return dx * dx + dy * dy + dz * dz;
 }
 
-__device__ __forceinline__ float nearest_leaf_bound(const SceneView& sc, const vec3f& q) {
+// Lower bound on the distance from q to the triangles of one leaf: the
+// leaf box distance, raised to the smallest distance from q to the leaf's
+// triangle planes minus the culling margin (a triangle lies in its plane).
+__device__ __forceinline__ float leaf_bound2(const SceneView& sc, int first, int count, float box_d2,
+                                             const vec3f& q, float margin) {
+  float pmin = 3.0e38f;
+  for (int i = 0; i < count; ++i) {
+    const float4 A = sc.tris[3 * (first + i)];
+    const vec3f n = wgsl::cross(xyz(sc.tris[3 * (first + i) + 1]), xyz(sc.tris[3 * (first + i) + 2]));
+    const vec3f d = q - xyz(A);
+    // a degenerate triangle gives NaN here, which fmaxf turns into 0
+    const float pd = fabsf(wgsl::dot(d, n)) * rsqrtf(wgsl::dot(n, n)) - margin;
+    pmin = fminf(pmin, fmaxf(pd, 0.0f));
+  }
+  return fmaxf(box_d2, pmin * pmin);
+}
+
+__device__ __forceinline__ float nearest_leaf_bound(const SceneView& sc, const vec3f& q, float margin) {
   float best = 3.0e38f;  // squared distance
   int stack[LINON_BVH_STACK];
   int sp = 0;
@@ -167,7 +185,7 @@ __device__ __forceinline__ float nearest_leaf_bound(const SceneView& sc, const v
       const float4 hi = sc.nodes[2 * node + 1];
       const int count = __float_as_int(hi.w);
       if (count > 0) {
-        best = nd;
+        best = fminf(best, leaf_bound2(sc, __float_as_int(lo.w), count, nd, q, margin));
       } else {
         const int first = __float_as_int(lo.w);
         const float d0 = box_dist2(sc.nodes[2 * first], sc.nodes[2 * first + 1], q);
@@ -269,7 +287,8 @@ struct RayState {
   float t, ct;          // time and its Kahan carry
   float h, last_diff;
   wgsl::vec4f color;
-  float safe;           // distance the ray may travel before it must be tested again
+  vec3f q0;             // centre of the current safe ball
+  float safe2;          // its squared radius (< 0: no ball)
   int face;
   int steps;
   int cool;             // steps left before the next safe-distance query
@@ -290,7 +309,8 @@ __device__ __forceinline__ void ray_init(RayState& r, const vec3f& origin, const
   r.color = wgsl::vec4f(0.0f, 0.0f, 0.0f, 0.0f);
   r.face = -1;
   r.steps = 0;
-  r.safe = 0.0f;
+  r.q0 = origin;
+  r.safe2 = -1.0f;
   r.cool = 0;
   r.has_color = false;
 }
@@ -334,35 +354,37 @@ __device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevM
   r.dir = (1.0f - w) * r.dir + w * v;
   const vec3f step_dir = r.dir * h;
   if (!r.has_color) {
-    // Safe-distance skip (BVH scenes): the L1 length bounds the segment's
-    // Euclidean length, so a segment within the remaining safe distance of
-    // its start cannot reach any leaf box and needs no test.
-    const float reach = fabsf(step_dir.x) + fabsf(step_dir.y) + fabsf(step_dir.z);
-    if (sc.n_nodes > 0 && reach <= r.safe) {
-      r.safe -= reach;
-    } else {
+    // Safe-ball skip (BVH scenes): every point within the ball of radius
+    // sqrt(safe2) around q0 is farther than the culling margin from every
+    // triangle, and a segment whose ends both lie in the ball lies in it
+    // (the ball is convex; the start was checked by the previous step), so
+    // such a segment cannot hit anything the brute-force loop would hit.
+    const vec3f seg_end = r.p + step_dir;
+    const vec3f dq = seg_end - r.q0;
+    if (!(sc.n_nodes > 0 && wgsl::dot(dq, dq) <= r.safe2)) {
       const float len = wgsl::length(step_dir);
 #if defined(LINON_PRECISE)
       const vec3f dirn = step_dir / len;
 #else
       const vec3f dirn = wgsl::normalize(step_dir);
 #endif
-      const vec3f seg_end = r.p + step_dir;
       HitRec hit = intersect_segment(sc, r.p, dirn, len, seg_end, err);
       if (hit.t > 0.0f && hit.t < len) {
         r.color = shade_hit(sc, hit, dirn);
         r.has_color = r.color.w > 0.0f;
         if (r.has_color) r.face = hit.id;
       }
-      r.safe = 0.0f;
+      r.safe2 = -1.0f;
       if (!r.has_color && sc.n_nodes > 0) {
         if (r.cool > 0) {
           r.cool--;
         } else {
-          // bound from the segment's end, where the next segment starts
-          r.safe = nearest_leaf_bound(sc, seg_end);
-          // close to geometry the bound buys little: test plainly for a while
-          if (r.safe < 4.0f * reach) r.cool = 8;
+          // a new ball around the segment's end, where the next one starts
+          const float b = nearest_leaf_bound(sc, seg_end, sc.margin);
+          r.q0 = seg_end;
+          r.safe2 = b * b;
+          // close to geometry the ball buys little: test plainly for a while
+          if (b < 4.0f * len) r.cool = 8;
         }
       }
     }
@@ -470,6 +492,7 @@ __device__ __forceinline__ SceneView cta_scene(const DevScene& s, float4* smem,
   v.face_rgb = s.face_rgb;
   v.n_tris = s.n_tris;
   v.n_nodes = s.n_nodes;
+  v.margin = s.margin;
   if (s.staged_bytes > 0) {
     // staged block = [nodes | tris] contiguous in global memory
     if (stage_to_smem(smem, s.staged, (unsigned)s.staged_bytes, mbar, err)) {

@@ -40,7 +40,7 @@ struct DevScene {
   int n_tris;
   int n_nodes;
   int staged_bytes;        // 0 = read the scene from global memory
-  int pad;
+  float margin;            // inflation of the BVH boxes (culling margin)
 };
 
 struct DevFrame {

@@ -537,20 +537,39 @@ template <int N> WG_HD bool any(const vec<bool, N>& v) {
 // ---------------------------------------------------------------------------
 #define LINON_PI 3.14159265358979323846f
 
+// The rotations are the shader's matrix products.  Precise modules (and the
+// host build) multiply out the full matrix, zero entries included; fast
+// modules drop the products with the structural zeros and ones, which
+// changes the result only for non-finite components (0 * inf).
+#if defined(LINON_PRECISE) || !defined(__CUDA_ARCH__)
+#define LINON_FULL_ROTATIONS 1
+#endif
 WG_HD vec3f rotateX(const vec3f& v, float phi) {  // main_view.wgsl:78-84
   float s, c;
   sincos_(phi, &s, &c);
+#ifdef LINON_FULL_ROTATIONS
   return make_mat(vec3f(1.0f, 0.0f, 0.0f), vec3f(0.0f, c, s), vec3f(0.0f, -s, c)) * v;
+#else
+  return vec3f(v.x, c * v.y - s * v.z, s * v.y + c * v.z);
+#endif
 }
 WG_HD vec3f rotateY(const vec3f& v, float phi) {  // main_view.wgsl:86-92
   float s, c;
   sincos_(phi, &s, &c);
+#ifdef LINON_FULL_ROTATIONS
   return make_mat(vec3f(c, 0.0f, -s), vec3f(0.0f, 1.0f, 0.0f), vec3f(s, 0.0f, c)) * v;
+#else
+  return vec3f(c * v.x + s * v.z, v.y, c * v.z - s * v.x);
+#endif
 }
 WG_HD vec3f rotateZ(const vec3f& v, float phi) {  // main_view.wgsl:94-100: third column zero
   float s, c;
   sincos_(phi, &s, &c);
+#ifdef LINON_FULL_ROTATIONS
   return make_mat(vec3f(c, s, 0.0f), vec3f(-s, c, 0.0f), vec3f(0.0f, 0.0f, 0.0f)) * v;
+#else
+  return vec3f(c * v.x - s * v.y, s * v.x + c * v.y, 0.0f);
+#endif
 }
 WG_HD vec3f translate(const vec3f& v, float dx, float dy, float dz) {  // main_view.wgsl:102-108
   return vec3f(v.x + dx, v.y + dy, v.z + dz);

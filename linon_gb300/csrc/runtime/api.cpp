@@ -115,7 +115,7 @@ DevScene dev_scene(const linon_ctx* ctx) {
   s.n_tris = ctx->n_tris;
   s.n_nodes = ctx->n_nodes;
   s.staged_bytes = ctx->staged_bytes;
-  s.pad = 0;
+  s.margin = ctx->margin;
   return s;
 }
 
@@ -390,6 +390,7 @@ int linon_scene_upload(linon_ctx* ctx, const float* xyz, uint32_t n_vertices, co
   ctx->n_tris = int(n_faces);
   ctx->n_nodes = int(b.nodes.size() / 2);
   ctx->max_depth = b.max_depth;
+  ctx->margin = b.margin;
   // small scenes are staged in shared memory by one TMA bulk copy per CTA
   ctx->staged_bytes = bytes <= 16384 && bytes > 0 ? int(bytes) : 0;
   ctx->has_scene = true;

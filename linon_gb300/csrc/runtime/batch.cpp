@@ -118,7 +118,7 @@ DevScene scene_of(const linon_ctx* ctx) {
   s.n_tris = ctx->n_tris;
   s.n_nodes = ctx->n_nodes;
   s.staged_bytes = ctx->staged_bytes;
-  s.pad = 0;
+  s.margin = ctx->margin;
   return s;
 }
 

@@ -185,6 +185,7 @@ void build_scene_arrays(const float* xyz, uint32_t nv, const uint32_t* abc, uint
   B.build(0, 0, nf, 0);
   out.nodes = std::move(B.nodes);
   out.max_depth = B.max_depth;
+  out.margin = B.margin;
   for (uint32_t i = 0; i < nf; ++i) push_tri(out.tris, xyz, abc, B.idx[i]);
 }
 

@@ -60,6 +60,7 @@ struct BvhBuild {
   std::vector<float4> nodes;   // 2 per node
   std::vector<float4> tris;    // 3 per triangle, leaf order
   uint32_t max_depth = 0;
+  float margin = 0.0f;         // inflation of the node boxes
 };
 // Builds the triangle array (brute force when leaf_size == 0) and, when
 // requested, a binned-SAH BVH whose node boxes are inflated by `margin`.
@@ -92,6 +93,7 @@ struct linon_ctx {
   linon::DevBuf face_rgb;
   int n_tris = 0, n_nodes = 0;
   uint32_t max_depth = 0;
+  float margin = 0.0f;
   int staged_bytes = 0;
   // device error word and scratch
   int* d_err = nullptr;

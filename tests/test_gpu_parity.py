@@ -141,9 +141,13 @@ def test_fast_math_accuracy(engine):
     assert (np.abs(out[:, 2] - ref) / np.maximum(ref, 1e-30)).max() <= 3.6e-7
 
 
-def test_bvh_equals_brute_force_cornell(engine):
+@pytest.mark.parametrize("name", ["twist", "lens", "lorenz_scaled"])
+def test_bvh_equals_brute_force_cornell(engine, name):
+    """BVH culling + safe-ball skipping vs the plain loop over all faces, on
+    fields whose rays travel far from (twist), orbit near (lens) and swirl
+    around (scaled Lorenz) the geometry."""
     w = wl.plain_small(256, 256)
-    fld = field(engine, "twist", False)
+    fld = field(engine, name, False)
     engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=False)
     a = gpu_render(engine, w, fld)
     engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
