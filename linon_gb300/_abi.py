@@ -108,6 +108,8 @@ PROTOTYPES = {
                                           i32, vp, vp]),
     "linon_capture_paths": (C.c_int, [vp, vp, P(Camera), P(Settings), P(MarchParams), i32, i32,
                                       vp, i32, C.c_float, i32, i32, vp]),
+    "linon_capture_paths_noalloc": (C.c_int, [vp, vp, P(Camera), P(Settings), P(MarchParams), i32, i32,
+                                              vp, i32, C.c_float, i32, i32, vp]),
     "linon_outline_select": (C.c_int, [vp, vp, i32, i32, C.c_float, vp, vp]),
     "linon_exponent_quantile": (C.c_int, [vp, vp, i32, i32, i32, C.c_double, P(C.c_float)]),
     "linon_outline_indices": (C.c_int, [vp, sz]),

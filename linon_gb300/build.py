@@ -37,7 +37,7 @@ CPP_SOURCES = [
     "runtime/api.cpp",
     "runtime/batch.cpp",
 ]
-CU_SOURCES = ["runtime/kernels.cu"]
+CU_SOURCES = ["runtime/kernels.cu", "runtime/noalloc.cu"]
 GENERATED = BUILD_DIR / "embedded_sources.cpp"
 
 CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
