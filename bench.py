@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     return ap.parse_args()
@@ -311,6 +313,10 @@ def main():
     if rank == 0 and not args.no_batch:
         result["batch_uneven_64"] = bench_batch(eng, stream, wl, torch, dev, predefined_source)
 
+    # ---- serving: Poisson request stream, continuous batching ----
+    if rank == 0 and not args.no_serve:
+        result["serving"] = bench_serving(eng, wl, predefined_source, args.serve_seconds)
+
     # ---- CPU baseline (oracle port on this host's cores, bounded sample) ----
     if rank == 0 and world == 1 and not args.no_cpu:
         v, threads, sample = cpu_baseline(pyoracle, w)
@@ -320,6 +326,30 @@ def main():
     eng.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+def bench_serving(eng, wl, predefined_source, seconds):
+    """Poisson 200 req/s (seeded) of frames 256^2..1920x1080 (60%), Enhance at
+    h/4 (15%), 1024^2 FP64 Lyapunov overlays (10%) and 16x16-ray captures with
+    4000-point polylines (15%), field switched every 5 s, over the Cornell room
+    + four icospheres behind the BVH; 40 GB budget for request outputs."""
+    from linon_gb300 import serving
+    w = wl.batch_uneven(1, seed=0)
+    eng.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    flds = [eng.compile_field(predefined_source(fid)) for fid in w.fields]
+    arrivals = serving.request_stream(duration_s=seconds, rate=200.0, seed=0)
+    srv = serving.Server(eng, flds, hbm_budget=40 << 30, slots=3)
+    try:
+        # warm the batch module and pool outside the measurement
+        serving.replay(srv, serving.request_stream(duration_s=0.25, rate=200.0, seed=99))
+        records = serving.replay(srv, arrivals)
+        stats = srv.stats()
+    finally:
+        srv.stop()
+    s = serving.summarize(records)
+    s.update({"rate_req_per_s": 200.0, "duration_s": seconds, "hbm_budget_bytes": 40 << 30, "slots": 3,
+              "bytes_peak": stats["bytes_peak"], "latency": "submit -> completion seen by the server (host clock)"})
+    return s
 
 
 def bench_batch(eng, stream, wl, torch, dev, predefined_source):

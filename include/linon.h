@@ -321,6 +321,76 @@ int linon_autotune_batch(linon_ctx* ctx, const linon_field* const* fields,
                          int32_t n_views, linon_batch_tuning* best,
                          double* best_ms);
 
+/* ---- serving: continuous batching of requests ---------------------------
+ * A server owns a scheduler thread and the context (do not use the context
+ * from other threads while it runs).  Requests of any kind and size are
+ * queued at submit, admitted in arrival order as their output memory fits the
+ * HBM budget, and launched in waves: all frames / Enhance re-renders /
+ * overlay renders admitted together go into one persistent batched launch,
+ * overlays and captures follow on the wave's streams.  `slots` waves can be
+ * on the GPU at once, so requests arriving while others run start without
+ * waiting for them.  Results stay in device memory until released.        */
+enum linon_request_kind {
+  LINON_REQ_FRAME = 0,    /* ray-cast frame (Enhance: smaller h_initial)    */
+  LINON_REQ_OVERLAY = 1,  /* frame + Lyapunov overlay (exponents)           */
+  LINON_REQ_CAPTURE = 2   /* ray-sample capture: n_rays full polylines      */
+};
+typedef struct linon_request {
+  int32_t kind;
+  int32_t field_index;          /* into the server's field table            */
+  linon_camera camera;
+  linon_settings settings;
+  linon_march_params params;
+  int32_t width, height;
+  int32_t fp64_overlay;         /* overlay: FP64 differencing               */
+  int32_t n_rays;               /* capture: rays at pos_xy (host, n_rays*2, */
+  int32_t n_steps;              /*   copied at submit), n_steps of size h,  */
+  int32_t record_every;         /*   one point every record_every steps     */
+  float h;
+  int32_t reserved;
+  const float* pos_xy;
+} linon_request;
+typedef struct linon_serve_config {
+  size_t hbm_budget;            /* bytes of request outputs (0 = unlimited) */
+  int32_t slots;                /* waves in flight (default 2)              */
+  int32_t max_wave;             /* requests per wave (default 256)          */
+  linon_batch_tuning tuning;    /* of the batched launch (zeros = auto)     */
+} linon_serve_config;
+typedef struct linon_result {
+  int32_t status;               /* LINON_OK done, LINON_EBUSY queued or
+                                   running, else the request's error        */
+  int32_t kind;
+  double t_submit_ms, t_admit_ms, t_done_ms;  /* server clock              */
+  int64_t ray_steps;            /* accepted RK4 steps of the request        */
+  linon_frame frame;            /* device planes (frames, overlays)         */
+  uint8_t* overlay;             /* overlay target rgba8 (device)            */
+  float* exponents;             /* overlay exponents (device)               */
+  float* paths;                 /* capture: n_rays * n_points float4        */
+  int32_t n_points;
+  int32_t wave;                 /* wave the request ran in                  */
+} linon_result;
+typedef struct linon_serve_counters {
+  uint64_t submitted, completed, failed, waves;
+  size_t bytes_in_use, bytes_peak;
+} linon_serve_counters;
+typedef struct linon_server linon_server;
+int linon_serve_start(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fields,
+                      const linon_serve_config* cfg, linon_server** out);
+int linon_serve_submit(linon_server* server, const linon_request* req, uint64_t* id);
+/* Non-blocking; out->status is LINON_EBUSY while the request is pending.  */
+int linon_serve_poll(linon_server* server, uint64_t id, linon_result* out);
+/* Waits at most timeout_ms; LINON_ETIMEOUT if the request is still pending. */
+int linon_serve_wait(linon_server* server, uint64_t id, double timeout_ms, linon_result* out);
+/* Copies one output plane of a finished request into dst (host or device
+ * memory, cudaMemcpyDefault), synchronously.  plane: 0 color, 1 mapping,
+ * 2 hit_id, 3 steps, 4 overlay target, 5 exponents, 6 capture paths.       */
+int linon_serve_copy(linon_server* server, uint64_t id, int32_t plane, void* dst, size_t bytes);
+/* Frees the request's device outputs (after it finished).                 */
+int linon_serve_release(linon_server* server, uint64_t id);
+int linon_serve_stats(linon_server* server, linon_serve_counters* out);
+/* Finishes the waves on the GPU, fails still-queued requests, joins.      */
+int linon_serve_stop(linon_server* server);
+
 /* ---- measurement -------------------------------------------------------
  * Measured FP32 throughput of the device (independent FFMA chains on every
  * SM, best of 5 launches timed with CUDA events), in TFLOP/s.             */

@@ -71,6 +71,34 @@ class BatchTuning(C.Structure):
                 ("tile_w", C.c_int32), ("tile_h", C.c_int32)]
 
 
+LINON_REQ_FRAME, LINON_REQ_OVERLAY, LINON_REQ_CAPTURE = 0, 1, 2
+
+
+class Request(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("field_index", C.c_int32), ("camera", Camera), ("settings", Settings),
+                ("params", MarchParams), ("width", C.c_int32), ("height", C.c_int32),
+                ("fp64_overlay", C.c_int32), ("n_rays", C.c_int32), ("n_steps", C.c_int32),
+                ("record_every", C.c_int32), ("h", C.c_float), ("reserved", C.c_int32),
+                ("pos_xy", C.c_void_p)]
+
+
+class ServeConfig(C.Structure):
+    _fields_ = [("hbm_budget", C.c_size_t), ("slots", C.c_int32), ("max_wave", C.c_int32),
+                ("tuning", BatchTuning)]
+
+
+class Result(C.Structure):
+    _fields_ = [("status", C.c_int32), ("kind", C.c_int32), ("t_submit_ms", C.c_double),
+                ("t_admit_ms", C.c_double), ("t_done_ms", C.c_double), ("ray_steps", C.c_int64),
+                ("frame", Frame), ("overlay", C.c_void_p), ("exponents", C.c_void_p), ("paths", C.c_void_p),
+                ("n_points", C.c_int32), ("wave", C.c_int32)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("waves", C.c_uint64), ("bytes_in_use", C.c_size_t), ("bytes_peak", C.c_size_t)]
+
+
 assert C.sizeof(Camera) == 112 and C.sizeof(Settings) == 24 and C.sizeof(RaySample) == 32
 assert C.sizeof(MarchParams) == 48
 
@@ -117,6 +145,14 @@ PROTOTYPES = {
     "linon_render_views_plain": (C.c_int, [vp, vp, i32, vp, i32]),
     "linon_autotune_batch": (C.c_int, [vp, vp, i32, vp, i32, P(BatchTuning), P(C.c_double)]),
     "linon_probe_fp32_peak": (C.c_int, [vp, P(C.c_double)]),
+    "linon_serve_start": (C.c_int, [vp, vp, i32, P(ServeConfig), P(vp)]),
+    "linon_serve_submit": (C.c_int, [vp, P(Request), P(C.c_uint64)]),
+    "linon_serve_poll": (C.c_int, [vp, C.c_uint64, P(Result)]),
+    "linon_serve_wait": (C.c_int, [vp, C.c_uint64, C.c_double, P(Result)]),
+    "linon_serve_copy": (C.c_int, [vp, C.c_uint64, i32, vp, sz]),
+    "linon_serve_release": (C.c_int, [vp, C.c_uint64]),
+    "linon_serve_stats": (C.c_int, [vp, P(ServeStats)]),
+    "linon_serve_stop": (C.c_int, [vp]),
 }
 
 _lib = None

@@ -36,6 +36,7 @@ CPP_SOURCES = [
     "runtime/bvh.cpp",
     "runtime/api.cpp",
     "runtime/batch.cpp",
+    "runtime/serve.cpp",
 ]
 CU_SOURCES = ["runtime/kernels.cu", "runtime/noalloc.cu"]
 GENERATED = BUILD_DIR / "embedded_sources.cpp"

@@ -156,6 +156,87 @@ int validate_batch(const linon_ctx* ctx, const linon_field* const* fields, int32
 
 }  // namespace
 
+int batch_tuning(const linon_ctx* ctx, const linon_batch_tuning* in, linon_batch_tuning& t) {
+  t = linon_batch_tuning{};
+  if (in) t = *in;
+  else if (ctx->has_tuned) t = ctx->tuned;
+  if (t.quantum <= 0) t.quantum = 32;
+  if (t.block_threads <= 0) t.block_threads = 128;
+  if (t.block_threads % 32 || t.block_threads > 256)
+    return set_error(LINON_EINVAL, "block_threads must be a multiple of 32, <= 256");
+  if (t.tile_w <= 0 || t.tile_h <= 0) {
+    t.tile_w = 8;
+    t.tile_h = 4;
+  }
+  if (t.tile_w * t.tile_h != 32) return set_error(LINON_EINVAL, "tile_w * tile_h must be 32");
+  return LINON_OK;
+}
+
+long long batch_table(const linon_view* views, int n_views, const linon_batch_tuning& t,
+                      std::vector<BatchView>& tab) {
+  tab.assign(static_cast<size_t>(n_views), BatchView());
+  long long begin = 0;
+  for (int i = 0; i < n_views; ++i) {
+    const linon_view& v = views[i];
+    BatchView& b = tab[size_t(i)];
+    b.m = to_dev(v.settings, v.params);
+    for (int k = 0; k < 3; ++k) {
+      b.cam.o[k] = v.camera.origin[k];
+      b.cam.d[k] = v.camera.view_direction[k];
+      b.cam.u[k] = v.camera.up[k];
+    }
+    b.field = v.field_index;
+    b.tiles_x = (v.width + t.tile_w - 1) / t.tile_w;
+    const int tiles_y = (v.height + t.tile_h - 1) / t.tile_h;
+    b.ray_begin = begin;
+    b.frame.W = v.width;
+    b.frame.H = v.height;
+    b.frame.color = reinterpret_cast<uchar4*>(v.out.color);
+    b.frame.mapping = reinterpret_cast<float4*>(v.out.mapping);
+    b.frame.hit = v.out.hit_id;
+    b.frame.steps = v.out.steps;
+    begin += (long long)b.tiles_x * tiles_y * 32;
+  }
+  return begin;
+}
+
+int batch_module(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fields,
+                 std::shared_ptr<JitModule>& mod) {
+  std::lock_guard<std::mutex> lock(g_bmu);
+  return get_module(ctx, g_batch[ctx], fields, n_fields, mod);
+}
+
+int batch_launch(linon_ctx* ctx, const std::shared_ptr<JitModule>& mod, const linon_batch_tuning& t,
+                 const BatchView* views_dev, int n_views, long long total_rays,
+                 unsigned long long* counter, cudaStream_t stream) {
+  BatchArgs a;
+  std::memset(&a, 0, sizeof a);
+  a.views = views_dev;
+  a.n_views = n_views;
+  a.quantum = t.quantum;
+  a.total_rays = total_rays;
+  a.counter = counter;
+  a.scene = scene_of(ctx);
+  a.tile_w = t.tile_w;
+  a.tile_h = t.tile_h;
+  a.err = ctx->d_err;
+  cudaKernel_t k = mod->kernels.at("linon_batch");
+  int sms = 0;
+  LINON_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  int per_sm = t.ctas_per_sm;
+  if (per_sm <= 0) {
+    int occ = 0;
+    LINON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)k, t.block_threads,
+                                                             size_t(a.scene.staged_bytes)));
+    per_sm = std::max(1, occ);
+  }
+  LINON_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream));
+  void* args[] = {&a};
+  LINON_CUDA(cudaLaunchKernel((const void*)k, dim3(unsigned(sms * per_sm)), dim3(unsigned(t.block_threads)), args,
+                              size_t(a.scene.staged_bytes), stream));
+  return LINON_OK;
+}
+
 void batch_release(linon_ctx* ctx) {
   std::lock_guard<std::mutex> lock(g_bmu);
   auto it = g_batch.find(ctx);
@@ -183,38 +264,10 @@ int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields, int32_t
     BatchState& bs = g_batch[ctx];
     std::shared_ptr<JitModule> mod;
     if (int st = get_module(ctx, bs, fields, n_fields, mod)) return st;
-    linon_batch_tuning t{};
-    if (tuning) t = *tuning;
-    else if (ctx->has_tuned) t = ctx->tuned;
-    if (t.quantum <= 0) t.quantum = 32;
-    if (t.block_threads <= 0) t.block_threads = 128;
-    if (t.block_threads % 32 || t.block_threads > 256) return set_error(LINON_EINVAL, "block_threads must be a multiple of 32, <= 256");
-    if (t.tile_w <= 0 || t.tile_h <= 0) { t.tile_w = 8; t.tile_h = 4; }
-    if (t.tile_w * t.tile_h != 32) return set_error(LINON_EINVAL, "tile_w * tile_h must be 32");
-    // view table
-    std::vector<BatchView> tab(static_cast<size_t>(n_views));
-    long long begin = 0;
-    for (int i = 0; i < n_views; ++i) {
-      const linon_view& v = views[i];
-      BatchView& b = tab[size_t(i)];
-      b.m = to_dev(v.settings, v.params);
-      for (int k = 0; k < 3; ++k) {
-        b.cam.o[k] = v.camera.origin[k];
-        b.cam.d[k] = v.camera.view_direction[k];
-        b.cam.u[k] = v.camera.up[k];
-      }
-      b.field = v.field_index;
-      b.tiles_x = (v.width + t.tile_w - 1) / t.tile_w;
-      const int tiles_y = (v.height + t.tile_h - 1) / t.tile_h;
-      b.ray_begin = begin;
-      b.frame.W = v.width;
-      b.frame.H = v.height;
-      b.frame.color = reinterpret_cast<uchar4*>(v.out.color);
-      b.frame.mapping = reinterpret_cast<float4*>(v.out.mapping);
-      b.frame.hit = v.out.hit_id;
-      b.frame.steps = v.out.steps;
-      begin += (long long)b.tiles_x * tiles_y * 32;
-    }
+    linon_batch_tuning t;
+    if (int st = batch_tuning(ctx, tuning, t)) return st;
+    std::vector<BatchView> tab;
+    const long long begin = batch_table(views, n_views, t, tab);
     if (int st = dev_grow(ctx, bs.views, sizeof(BatchView) * tab.size())) return st;
     if (int st = dev_grow(ctx, bs.counter, 256)) return st;
     LINON_CUDA(cudaMemcpyAsync(bs.views.p, tab.data(), sizeof(BatchView) * tab.size(),

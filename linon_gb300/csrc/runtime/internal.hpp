@@ -70,6 +70,16 @@ void build_scene_arrays(const float* xyz, uint32_t nv, const uint32_t* abc, uint
 // Frees the batch tables, graphs and modules of a context (batch.cpp).
 void batch_release(linon_ctx* ctx);
 
+// Pieces of the batched launch, shared with the serving loop (batch.cpp).
+int batch_tuning(const linon_ctx* ctx, const linon_batch_tuning* in, linon_batch_tuning& t);
+long long batch_table(const linon_view* views, int n_views, const linon_batch_tuning& t,
+                      std::vector<BatchView>& tab);
+int batch_module(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fields,
+                 std::shared_ptr<JitModule>& mod);
+int batch_launch(linon_ctx* ctx, const std::shared_ptr<JitModule>& mod, const linon_batch_tuning& t,
+                 const BatchView* views_dev, int n_views, long long total_rays,
+                 unsigned long long* counter, cudaStream_t stream);
+
 }  // namespace linon
 
 // ---- context and field objects (opaque in the ABI) ----------------------

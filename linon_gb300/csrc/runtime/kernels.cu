@@ -249,6 +249,15 @@ __global__ void pack_samples_kernel(const float4* pos, linon_ray_sample* out, in
   out[i] = s;
 }
 
+// Sum of a step-count plane (accepted RK4 steps of one frame).
+__global__ void sum_steps_kernel(const int* steps, long long n, unsigned long long* out) {
+  unsigned long long acc = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    acc += (unsigned long long)steps[i];
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
+}
+
 // FP32 throughput probe: independent FFMA chains per thread.
 __global__ void fp32_probe_kernel(float* out, int iters, float seed) {
   float a0 = seed + threadIdx.x, a1 = a0 + 1.0f, a2 = a0 + 2.0f, a3 = a0 + 3.0f;
@@ -303,6 +312,16 @@ cudaError_t launch_pack_samples(const float4* pos, linon_ray_sample* out, int n_
                                 cudaStream_t s) {
   const int n = n_rays * n_pts;
   pack_samples_kernel<<<(n + 255) / 256, 256, 0, s>>>(pos, out, n_rays, n_pts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sum_steps(const int* steps, long long n, unsigned long long* out, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks < 1) blocks = 1;
+  sum_steps_kernel<<<unsigned(blocks), 256, 0, s>>>(steps, n, out);
   return cudaGetLastError();
 }
 
