@@ -307,6 +307,7 @@ typedef struct linon_batch_tuning {
   int32_t block_threads;    /* threads per CTA (0 = auto)                  */
   int32_t ctas_per_sm;      /* resident CTAs per SM (0 = auto)             */
   int32_t tile_w, tile_h;   /* pixel tile handed out per queue pop (0=auto) */
+  int32_t refill_below;     /* refill early when fewer lanes march (0=auto) */
 } linon_batch_tuning;
 int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields,
                        int32_t n_fields, const linon_view* views,

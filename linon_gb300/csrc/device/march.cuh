@@ -663,11 +663,14 @@ __device__ __forceinline__ void march_batch_kernel(const Fields& fields, const B
       if (drained) break;
       continue;
     }
-    // ---- march a quantum (one warp vote per step keeps the lanes converged) ----
+    // ---- march a quantum (one warp vote per step keeps the lanes converged;
+    //      the warp leaves early to refill once fewer than refill_below lanes
+    //      are still marching and the queue has work) ----
     const FieldRef<Fields> field{fields, fidx};
     for (int q = 0; q < a.quantum; ++q) {
       const bool go = active && ray_active(r, m);
-      if (!__any_sync(FULL, go)) break;
+      const unsigned g = __ballot_sync(FULL, go);
+      if (g == 0u || (!drained && __popc(g) < a.refill_below)) break;
       if (go) ray_step_rt(r, field, m, sc, a.err);
     }
     if (active && !ray_active(r, m)) {

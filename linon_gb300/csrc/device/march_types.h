@@ -78,6 +78,8 @@ struct BatchArgs {
   unsigned long long* counter;  // queue head (zeroed before the launch)
   DevScene scene;
   int tile_w, tile_h;      // tile_w * tile_h == 32
+  int refill_below;        // leave the quantum early below this many marching lanes
+  int pad;
   int* err;
 };
 

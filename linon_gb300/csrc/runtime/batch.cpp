@@ -161,6 +161,8 @@ int batch_tuning(const linon_ctx* ctx, const linon_batch_tuning* in, linon_batch
   if (in) t = *in;
   else if (ctx->has_tuned) t = ctx->tuned;
   if (t.quantum <= 0) t.quantum = 32;
+  if (t.refill_below <= 0) t.refill_below = 24;
+  if (t.refill_below > 32) t.refill_below = 32;
   if (t.block_threads <= 0) t.block_threads = 128;
   if (t.block_threads % 32 || t.block_threads > 256)
     return set_error(LINON_EINVAL, "block_threads must be a multiple of 32, <= 256");
@@ -219,6 +221,7 @@ int batch_launch(linon_ctx* ctx, const std::shared_ptr<JitModule>& mod, const li
   a.scene = scene_of(ctx);
   a.tile_w = t.tile_w;
   a.tile_h = t.tile_h;
+  a.refill_below = t.refill_below;
   a.err = ctx->d_err;
   cudaKernel_t k = mod->kernels.at("linon_batch");
   int sms = 0;
@@ -282,6 +285,7 @@ int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields, int32_t
     a.scene = scene_of(ctx);
     a.tile_w = t.tile_w;
     a.tile_h = t.tile_h;
+    a.refill_below = t.refill_below;
     a.err = ctx->d_err;
     cudaKernel_t k = mod->kernels.at("linon_batch");
     int sms = 0;
@@ -340,9 +344,10 @@ int linon_autotune_batch(linon_ctx* ctx, const linon_field* const* fields, int32
                          const linon_view* views, int32_t n_views, linon_batch_tuning* best,
                          double* best_ms) {
   if (int st = validate_batch(ctx, fields, n_fields, views, n_views)) return st;
-  const int quanta[] = {8, 16, 32, 64};
-  const int blocks[] = {64, 128, 256};
-  const int tiles[][2] = {{8, 4}, {4, 8}, {16, 2}};
+  const int quanta[] = {16, 32, 64};
+  const int blocks[] = {128, 256};
+  const int tiles[][2] = {{8, 4}, {4, 8}};
+  const int refills[] = {16, 24, 28};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -350,12 +355,14 @@ int linon_autotune_batch(linon_ctx* ctx, const linon_field* const* fields, int32
   linon_batch_tuning bt{};
   for (int q : quanta)
     for (int b : blocks)
-      for (auto& tl : tiles) {
+      for (auto& tl : tiles)
+        for (int rf : refills) {
         linon_batch_tuning t{};
         t.quantum = q;
         t.block_threads = b;
         t.tile_w = tl[0];
         t.tile_h = tl[1];
+        t.refill_below = rf;
         if (int st = linon_render_batch(ctx, fields, n_fields, views, n_views, &t)) {
           cudaEventDestroy(e0);
           cudaEventDestroy(e1);
