@@ -161,7 +161,9 @@ int batch_tuning(const linon_ctx* ctx, const linon_batch_tuning* in, linon_batch
   if (in) t = *in;
   else if (ctx->has_tuned) t = ctx->tuned;
   if (t.quantum <= 0) t.quantum = 32;
-  if (t.refill_below <= 0) t.refill_below = 24;
+  // 0: refill only at the end of a quantum (measured best on the 64-view
+  // workload: an early refill costs a queue atomic and a camera set-up)
+  if (t.refill_below < 0) t.refill_below = 0;
   if (t.refill_below > 32) t.refill_below = 32;
   if (t.block_threads <= 0) t.block_threads = 128;
   if (t.block_threads % 32 || t.block_threads > 256)
@@ -347,7 +349,7 @@ int linon_autotune_batch(linon_ctx* ctx, const linon_field* const* fields, int32
   const int quanta[] = {16, 32, 64};
   const int blocks[] = {128, 256};
   const int tiles[][2] = {{8, 4}, {4, 8}};
-  const int refills[] = {16, 24, 28};
+  const int refills[] = {0, 16, 24};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);

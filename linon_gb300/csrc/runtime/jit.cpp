@@ -51,6 +51,11 @@ std::vector<std::string> options(bool precise) {
   if (precise) {
     o.push_back("--fmad=false");
     o.push_back("-DLINON_PRECISE=1");
+  } else {
+    // fast modules: the hardware reciprocal / square-root sequences (about
+    // 1 ulp) instead of the correctly rounded ones
+    o.push_back("--prec-div=false");
+    o.push_back("--prec-sqrt=false");
   }
   if (std::getenv("LINON_JIT_VERBOSE")) o.push_back("--ptxas-options=--verbose");
   return o;
