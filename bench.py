@@ -313,6 +313,10 @@ def main():
     if rank == 0 and not args.no_batch:
         result["batch_uneven_64"] = bench_batch(eng, stream, wl, torch, dev, predefined_source)
 
+    # ---- Lyapunov pipeline at 1024^2 (scaled Lorenz + v0, h 0.002 x 2000) ----
+    if rank == 0 and not args.no_batch:
+        result["lyapunov_1024"] = bench_lyapunov(eng, wl, predefined_source)
+
     # ---- serving: Poisson request stream, continuous batching ----
     if rank == 0 and not args.no_serve:
         result["serving"] = bench_serving(eng, wl, predefined_source, args.serve_seconds)
@@ -326,6 +330,23 @@ def main():
     eng.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+def bench_lyapunov(eng, wl, predefined_source):
+    """Render + FP64 overlay + finite-time exponent (T = 4) + p95 threshold +
+    outline pixels + 8x100 outline capture, per-stage device ms (median of 3)."""
+    import torch
+    from linon_gb300 import lyapunov
+    w = wl.lyapunov_1024()
+    eng.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    fld = eng.compile_field(predefined_source(w.fields[0]))
+    with torch.cuda.stream(eng.stream):  # events and engine work on one stream
+        runs = [lyapunov.run(eng, fld, w, horizon=w.extra["T"], quantile=w.extra["quantile"], timings=True)
+                for _ in range(4)][1:]
+    ms = {k: statistics.median(r["ms"][k] for r in runs) for k in runs[0]["ms"]}
+    steps = int(runs[-1]["planes"].steps.sum().item())
+    return {"workload": w.name, "ms": ms, "total_ms": sum(ms.values()),
+            "render_ray_steps_per_s": steps / (ms["render"] * 1e-3), "threshold_p95": runs[-1]["threshold"]}
 
 
 def bench_serving(eng, wl, predefined_source, seconds):

@@ -73,13 +73,18 @@ class Engine:
     """One linon context on one CUDA device."""
 
     def __init__(self, device: int = 0, hbm_budget: int = 0, stream=None):
+        import torch
+        self._torch = torch
         self.lib = load()
         self.device = device
         ctx = C.c_void_p()
         check(self.lib.linon_create(device, hbm_budget, C.byref(ctx)))
         self.ctx = ctx
-        if stream is not None:
-            self.set_stream(stream)
+        # The engine enqueues on a torch stream of its own; every call is
+        # fenced against torch's current stream on entry and exit, so tensors
+        # torch produced are ready and results are ordered for torch users.
+        self.stream = None
+        self.set_stream(stream if stream is not None else torch.cuda.Stream(device=device))
 
     def close(self):
         if self.ctx:
@@ -93,9 +98,22 @@ class Engine:
             pass
 
     def set_stream(self, stream):
-        """stream: a torch.cuda.Stream, a raw cudaStream_t int, or None."""
-        raw = getattr(stream, "cuda_stream", stream)
-        check(self.lib.linon_set_stream(self.ctx, C.c_void_p(raw) if raw else None))
+        """stream: a torch.cuda.Stream (the engine's queue from now on)."""
+        self.stream = stream
+        # torch's default stream is the legacy default stream (handle 0); the
+        # ABI reads NULL as "the context's own stream", so pass
+        # cudaStreamLegacy (1) for it
+        raw = stream.cuda_stream if stream.cuda_stream else 1
+        check(self.lib.linon_set_stream(self.ctx, C.c_void_p(raw)))
+
+    def _call(self, name, *args):
+        cur = self._torch.cuda.current_stream(self.device)
+        fenced = cur.cuda_stream != self.stream.cuda_stream
+        if fenced:
+            self.stream.wait_stream(cur)
+        check(getattr(self.lib, name)(*args))
+        if fenced:
+            cur.wait_stream(self.stream)
 
     def synchronize(self):
         check(self.lib.linon_synchronize(self.ctx))
@@ -138,15 +156,15 @@ class Engine:
     # ---- the two dispatches of MainView::render ----
     def render(self, field: Field, camera, settings, params, frame: FramePlanes):
         f = frame.abi()
-        check(self.lib.linon_render(self.ctx, field.handle, C.byref(camera), C.byref(settings),
-                                    C.byref(params), C.byref(f)))
+        self._call("linon_render", self.ctx, field.handle, C.byref(camera), C.byref(settings),
+                                    C.byref(params), C.byref(f))
 
     def field_eval(self, field: Field, inputs):
         """Evaluates the field at n points (torch CUDA tensor [n, 13]) -> [n, 3]."""
         import torch
         x = inputs.contiguous().to(torch.float32)
         out = torch.empty((x.shape[0], 3), dtype=torch.float32, device=x.device)
-        check(self.lib.linon_field_eval(self.ctx, field.handle, x.data_ptr(), out.data_ptr(), x.shape[0]))
+        self._call("linon_field_eval", self.ctx, field.handle, x.data_ptr(), out.data_ptr(), x.shape[0])
         return out
 
     def render_host(self, field: Field, camera, settings, params, width: int, height: int,
@@ -163,21 +181,21 @@ class Engine:
             elif on is not None and on is not False:
                 out[name] = on
             ptr[name] = out[name].ctypes.data if name in out else None
-        check(self.lib.linon_render_host(self.ctx, field.handle, C.byref(camera), C.byref(settings),
+        self._call("linon_render_host", self.ctx, field.handle, C.byref(camera), C.byref(settings),
                                          C.byref(params), width, height, ptr["color"], ptr["mapping"],
-                                         ptr["hit_id"], ptr["steps"]))
+                                         ptr["hit_id"], ptr["steps"])
         return out
 
     def overlay(self, settings, width, height, ray_casting, mapping, target, exponents=None,
                 srgb=False, fp64=False):
-        check(self.lib.linon_overlay(self.ctx, C.byref(settings), width, height, ray_casting.data_ptr(),
+        self._call("linon_overlay", self.ctx, C.byref(settings), width, height, ray_casting.data_ptr(),
                                      mapping.data_ptr() if mapping is not None else None,
                                      target.data_ptr(), exponents.data_ptr() if exponents is not None else None,
-                                     1 if srgb else 0, 1 if fp64 else 0))
+                                     1 if srgb else 0, 1 if fp64 else 0)
 
     def ftle(self, camera, params, width, height, mapping, horizon, exponents):
-        check(self.lib.linon_ftle(self.ctx, C.byref(camera), C.byref(params), width, height,
-                                  mapping.data_ptr(), float(horizon), exponents.data_ptr()))
+        self._call("linon_ftle", self.ctx, C.byref(camera), C.byref(params), width, height,
+                                  mapping.data_ptr(), float(horizon), exponents.data_ptr())
 
     # ---- path capture (sample_rays) ----
     def capture_reference(self, field: Field, camera, settings, params, width, height, out,
@@ -185,30 +203,30 @@ class Engine:
         pos = None
         if positions is not None:
             pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(8, 2)
-        check(self.lib.linon_capture_reference(self.ctx, field.handle, C.byref(camera), C.byref(settings),
+        self._call("linon_capture_reference", self.ctx, field.handle, C.byref(camera), C.byref(settings),
                                                C.byref(params), width, height,
                                                pos.ctypes.data if pos is not None else None,
-                                               out.data_ptr()))
+                                               out.data_ptr())
 
     def capture_paths(self, field: Field, camera, settings, params, width, height, pos_xy, h, n_steps,
                       record_every, out):
         pos = np.ascontiguousarray(pos_xy, dtype=np.float32).reshape(-1, 2)
-        check(self.lib.linon_capture_paths(self.ctx, field.handle, C.byref(camera), C.byref(settings),
+        self._call("linon_capture_paths", self.ctx, field.handle, C.byref(camera), C.byref(settings),
                                            C.byref(params), width, height, pos.ctypes.data, len(pos),
-                                           float(h), int(n_steps), int(record_every), out.data_ptr()))
+                                           float(h), int(n_steps), int(record_every), out.data_ptr())
 
     # ---- outline rays ----
     def outline_select(self, exponents, width, height, min_exp=0.8):
         pix = np.zeros((8, 2), dtype=np.int32)
         pos = np.zeros((8, 2), dtype=np.float32)
-        check(self.lib.linon_outline_select(self.ctx, exponents.data_ptr(), width, height, float(min_exp),
-                                            pix.ctypes.data, pos.ctypes.data))
+        self._call("linon_outline_select", self.ctx, exponents.data_ptr(), width, height, float(min_exp),
+                                            pix.ctypes.data, pos.ctypes.data)
         return pix, pos
 
     def exponent_quantile(self, exponents, width, height, q, border=0):
         out = C.c_float()
-        check(self.lib.linon_exponent_quantile(self.ctx, exponents.data_ptr(), width, height, border,
-                                               float(q), C.byref(out)))
+        self._call("linon_exponent_quantile", self.ctx, exponents.data_ptr(), width, height, border,
+                                               float(q), C.byref(out))
         return out.value
 
     # ---- batches ----
@@ -219,19 +237,19 @@ class Engine:
 
     def render_batch(self, fields, views, tuning: _abi.BatchTuning | None = None):
         fa, va = self._batch_args(fields, views)
-        check(self.lib.linon_render_batch(self.ctx, fa, len(fields), va, len(views),
-                                          C.byref(tuning) if tuning is not None else None))
+        self._call("linon_render_batch", self.ctx, fa, len(fields), va, len(views),
+                                          C.byref(tuning) if tuning is not None else None)
 
     def render_views_plain(self, fields, views):
         fa, va = self._batch_args(fields, views)
-        check(self.lib.linon_render_views_plain(self.ctx, fa, len(fields), va, len(views)))
+        self._call("linon_render_views_plain", self.ctx, fa, len(fields), va, len(views))
 
     def autotune_batch(self, fields, views):
         fa, va = self._batch_args(fields, views)
         t = _abi.BatchTuning()
         ms = C.c_double()
-        check(self.lib.linon_autotune_batch(self.ctx, fa, len(fields), va, len(views), C.byref(t),
-                                            C.byref(ms)))
+        self._call("linon_autotune_batch", self.ctx, fa, len(fields), va, len(views), C.byref(t),
+                                            C.byref(ms))
         return t, ms.value
 
     def probe_fp32_peak(self) -> float:

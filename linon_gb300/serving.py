@@ -119,11 +119,13 @@ class Arrival:
 
 
 def request_stream(duration_s: float = 10.0, rate: float = 200.0, seed: int = 0, n_fields: int = 3,
-                   switch_s: float = 5.0, h: float = 0.01):
-    """Poisson arrivals at `rate`/s: 60% frames (256^2..1920x1080), 15% Enhance
-    (h/4), 10% 1024^2 Lyapunov overlays (FP64), 15% captures of 16x16 rays
-    around a clicked pixel with full polylines of 4000 points; the field
-    switches every `switch_s` seconds; cameras on the radius-3 sphere."""
+                   switch_s: float = 5.0, h: float = 0.02):
+    """Poisson arrivals at `rate`/s: 60% frames (256^2..1920x1080) at step h
+    for t <= 4, 15% Enhance re-renders at h/4, 10% 1024^2 Lyapunov overlays
+    (FP64), 15% captures of 16x16 rays around a clicked pixel with full
+    polylines of 4000 points; the field switches every `switch_s` seconds;
+    cameras on the radius-3 sphere.  The interactive step h = 0.02 is the
+    coarsest step of the batch workload (Enhance then runs 800 steps)."""
     rng = np.random.default_rng(seed)
     out = []
     t = 0.0
@@ -154,7 +156,7 @@ def request_stream(duration_s: float = 10.0, rate: float = 200.0, seed: int = 0,
             px, py = rng.integers(8, W - 8), rng.integers(8, H - 8)
             g = (np.arange(16) - 7.5) / (W - 1)
             pos = np.stack(np.meshgrid(px / (W - 1) + g, py / (H - 1) + g), -1).reshape(-1, 2).astype(np.float32)
-            p = wl.fixed_steps(h, 400)
+            p = wl.fixed_steps(h, int(round(4.0 / h)))
             out.append(Arrival(t, capture_request(fidx, camera, st, p, W, H, 0.001, 3999, 1), pos, "capture"))
     return out
 
