@@ -131,16 +131,16 @@ def cpu_baseline(pyoracle, w, budget_s=12.0):
     threads = pyoracle.max_threads()
     rng = np.random.default_rng(0)
     n_total = w.width * w.height
-    # calibrate on a small sample, then size the measured sample to the budget
-    pix = np.sort(rng.choice(n_total, size=256, replace=False)).astype(np.int32)
+    # calibrate on a sample that keeps every thread busy, then size the
+    # measured sample to the time budget
+    n_cal = min(n_total, 32 * threads)
+    pix = np.sort(rng.choice(n_total, size=n_cal, replace=False)).astype(np.int32)
     t0 = time.perf_counter()
-    steps = 0
     for fid in w.fields:
-        r = pyoracle.render(w.xyz, w.faces, w.face_rgb, w.camera, w.settings, w.params, fid, w.width, w.height,
-                            pixels=pix, threads=threads, want=("steps",))
-        steps += int(r["steps"].sum())
+        pyoracle.render(w.xyz, w.faces, w.face_rgb, w.camera, w.settings, w.params, fid, w.width, w.height,
+                        pixels=pix, threads=threads, want=("steps",))
     dt = time.perf_counter() - t0
-    n = int(min(n_total, max(256, 256 * budget_s / max(dt, 1e-3) * 0.8)))
+    n = int(min(n_total, max(n_cal, n_cal * budget_s / max(dt, 1e-3))))
     pix = np.sort(rng.choice(n_total, size=n, replace=False)).astype(np.int32)
     t0 = time.perf_counter()
     steps = 0

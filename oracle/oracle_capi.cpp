@@ -59,7 +59,7 @@ void render_impl(const Scene& sc, int field, const Camera& cam, const March& m, 
                  double* mapping64, int32_t* hit, int32_t* steps, int nthreads) {
   CameraBasis<T> b = camera_basis<T>(cam, W, H, m);
   const int64_t n = pixels ? npix : int64_t(W) * H;
-#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+#pragma omp parallel for schedule(dynamic, 8) num_threads(nthreads)
   for (int64_t i = 0; i < n; ++i) {
     int64_t pix = pixels ? pixels[i] : i;
     int row = int(pix / W), x = int(pix % W);
