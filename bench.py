@@ -301,7 +301,8 @@ def main():
                 traffic = None
         result["roofline"] = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                               "frac": achieved / peak, "traffic": traffic,
-                              "kernel": f"linon_march_a0_k1 ({['linear', 'twist', 'lens'][i]} field)",
+                              "kernel": f"linon_march_v14 ({['linear', 'twist', 'lens'][i]} field; "
+                                        "fixed steps, Kahan, field_weight 1)",
                               "peak_source": "measured FFMA probe in this run (linon_probe_fp32_peak)",
                               "flops_per_step": {n: round(a, 2) for n, (a, _) in zip(["linear", "twist", "lens"], fl)},
                               "transcendentals_per_step": {n: round(t, 2) for n, (_, t) in

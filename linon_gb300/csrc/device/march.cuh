@@ -324,15 +324,26 @@ __device__ __forceinline__ void kahan_add(float& sum, float& c, float x) {
 
 // Is the ray still marching?  (loop condition of main_view.wgsl:244, or the
 // fixed step budget, or the first hit with stop_on_hit)
+// LOOP: 0 decided at run time, 1 fixed step budget, 2 the t-loop.
+template <int LOOP = 0>
 __device__ __forceinline__ bool ray_active(const RayState& r, const DevMarch& m) {
   if (m.stop_on_hit && r.has_color) return false;
+  if (LOOP == 1) return r.steps < m.max_steps;
+  if (LOOP == 2) return r.t <= m.t_max;
   if (m.max_steps > 0) return r.steps < m.max_steps;
   return r.t <= m.t_max;
 }
 
+// Variant bits of the specialised march kernels (one NVRTC kernel per used
+// combination): adaptive refinement, Kahan sums, fixed step budget (with it
+// the compiler drops the time accumulator when the field ignores t), and
+// field_weight == 1 in fast modules (the blend is then dir = v, identical
+// for finite directions).
+enum { V_ADAPTIVE = 1, V_KAHAN = 2, V_STEPS = 4, V_W1 = 8 };
+
 // One attempted RK4 step (main_view.wgsl:245-270).  Returns false when the
 // step was rejected by the adaptive rule (h refined, nothing advanced).
-template <bool ADAPTIVE, bool KAHAN, class F>
+template <bool ADAPTIVE, bool KAHAN, bool W1 = false, class F>
 __device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevMarch& m,
                                          const SceneView& sc, int* err) {
   const float h = r.h;
@@ -350,8 +361,12 @@ __device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevM
       return false;
     }
   }
-  const float w = m.field_weight;
-  r.dir = (1.0f - w) * r.dir + w * v;
+  if (W1) {
+    r.dir = v;
+  } else {
+    const float w = m.field_weight;
+    r.dir = (1.0f - w) * r.dir + w * v;
+  }
   const vec3f step_dir = r.dir * h;
   if (!r.has_color) {
     // Safe-ball skip (BVH scenes): every point within the ball of radius
@@ -508,8 +523,17 @@ __device__ __forceinline__ SceneView cta_scene(const DevScene& s, float4* smem,
 // --------------------------------------------------------------------------
 
 // One thread per pixel; the CTA covers a tile_w x tile_h pixel tile.
-template <bool ADAPTIVE, bool KAHAN, class F>
+// V: variant bits (V_ADAPTIVE | V_KAHAN | V_STEPS | V_W1).
+template <int V, class F>
 __device__ __forceinline__ void march_plain_kernel(const F& field, const MarchArgs& a) {
+  constexpr bool ADAPTIVE = (V & V_ADAPTIVE) != 0;
+  constexpr bool KAHAN = (V & V_KAHAN) != 0;
+  constexpr int LOOP = (V & V_STEPS) ? 1 : 2;
+#if defined(LINON_PRECISE)
+  constexpr bool W1 = false;  // op-for-op modules keep the shader's blend
+#else
+  constexpr bool W1 = (V & V_W1) != 0;
+#endif
   extern __shared__ float4 linon_smem[];
   __shared__ unsigned long long mbar;
   const SceneView sc = cta_scene(a.scene, linon_smem, &mbar, a.err);
@@ -544,11 +568,11 @@ __device__ __forceinline__ void march_plain_kernel(const F& field, const MarchAr
   // The vote at the top of every step reconverges the warp: without it the
   // lanes that diverged at a (rare) intersection test would walk the rest of
   // the march separately, a few lanes per issued instruction.
-  bool active = in_image && ray_active(r, a.m);
+  bool active = in_image && ray_active<LOOP>(r, a.m);
   while (__any_sync(0xffffffffu, active)) {
     if (active) {
-      ray_step<ADAPTIVE, KAHAN>(r, field, a.m, sc, a.err);
-      active = ray_active(r, a.m);
+      ray_step<ADAPTIVE, KAHAN, W1>(r, field, a.m, sc, a.err);
+      active = ray_active<LOOP>(r, a.m);
     }
   }
   if (in_image) ray_store(r, a.frame, idx);

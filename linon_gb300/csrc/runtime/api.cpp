@@ -146,8 +146,23 @@ int check_params(const linon_march_params* mp) {
   return LINON_OK;
 }
 
+// The march variant a render needs (bits of march.cuh's V_* enum).
+int march_variant(const linon_march_params* mp, const linon_settings* st, bool precise) {
+  int v = 0;
+  if (mp->adaptive) v |= 1;
+  if (mp->kahan) v |= 2;
+  if (mp->max_steps > 0) v |= 4;
+  if (!precise && (st ? st->field_weight : 1.0f) == 1.0f) v |= 8;
+  return v;
+}
+
+std::string march_kernel_name(int v) { return "linon_march_v" + std::to_string(v); }
+
 // Module source for one field: generated CUDA C + the kernel instantiations.
-std::string module_source(const std::string& field_cuda) {
+// The base module holds the capture and field-evaluation kernels and the
+// march variant of the reference's own settings; other march variants are
+// compiled into small modules of their own when a render first needs them.
+std::string module_source(const std::string& field_cuda, const std::vector<int>& variants, bool base) {
   std::ostringstream s;
   s << "#include \"march.cuh\"\n" << field_cuda << R"LINON(
 struct LinonField {
@@ -156,19 +171,12 @@ struct LinonField {
     return linon_user::field_function(pp, p, v0, v, t);
   }
 };
-extern "C" __global__ void __launch_bounds__(128) linon_march_a0_k0(linon::MarchArgs a) {
-  linon::march_plain_kernel<false, false>(LinonField(), a);
-}
-extern "C" __global__ void __launch_bounds__(128) linon_march_a0_k1(linon::MarchArgs a) {
-  linon::march_plain_kernel<false, true>(LinonField(), a);
-}
-extern "C" __global__ void __launch_bounds__(128) linon_march_a1_k0(linon::MarchArgs a) {
-  linon::march_plain_kernel<true, false>(LinonField(), a);
-}
-extern "C" __global__ void __launch_bounds__(128) linon_march_a1_k1(linon::MarchArgs a) {
-  linon::march_plain_kernel<true, true>(LinonField(), a);
-}
-extern "C" __global__ void __launch_bounds__(256) linon_capture(linon::CaptureArgs a) {
+)LINON";
+  for (int v : variants)
+    s << "extern \"C\" __global__ void __launch_bounds__(128) " << march_kernel_name(v)
+      << "(linon::MarchArgs a) {\n  linon::march_plain_kernel<" << v << ">(LinonField(), a);\n}\n";
+  if (base)
+    s << R"LINON(extern "C" __global__ void __launch_bounds__(256) linon_capture(linon::CaptureArgs a) {
   linon::capture_kernel(LinonField(), a);
 }
 extern "C" __global__ void __launch_bounds__(256) linon_field_eval(const float* in, float* out, int n) {
@@ -178,11 +186,41 @@ extern "C" __global__ void __launch_bounds__(256) linon_field_eval(const float* 
   return s.str();
 }
 
-const std::vector<std::string>& module_kernels() {
-  static const std::vector<std::string> k = {"linon_march_a0_k0", "linon_march_a0_k1",
-                                             "linon_march_a1_k0", "linon_march_a1_k1",
-                                             "linon_capture",     "linon_field_eval"};
+std::vector<std::string> module_kernels(const std::vector<int>& variants, bool base) {
+  std::vector<std::string> k;
+  for (int v : variants) k.push_back(march_kernel_name(v));
+  if (base) {
+    k.push_back("linon_capture");
+    k.push_back("linon_field_eval");
+  }
   return k;
+}
+
+// Base variant: the reference's t <= 5 loop with adaptive refinement,
+// field_weight 1 (main_view.wgsl:227-244, main_view.rs:133-139).
+int base_variant(bool precise) { return precise ? 1 : 1 | 8; }
+
+// Kernel of march variant v for the field, compiling it on first use.
+int march_kernel(const linon_field* f, int v, cudaKernel_t* out) {
+  {
+    auto it = f->mod->kernels.find(march_kernel_name(v));
+    if (it != f->mod->kernels.end()) {
+      *out = it->second;
+      return LINON_OK;
+    }
+  }
+  std::lock_guard<std::mutex> lock(f->vmu);
+  auto vit = f->variants.find(v);
+  if (vit == f->variants.end()) {
+    std::shared_ptr<JitModule> mod;
+    std::string log;
+    const bool precise = (f->flags & LINON_COMPILE_PRECISE) != 0;
+    int st = jit_compile(module_source(f->cuda, {v}, false), precise, module_kernels({v}, false), mod, log);
+    if (st != LINON_OK) return set_error(st, st == LINON_ECOMPILE ? log : std::string(g_last_error));
+    vit = f->variants.emplace(v, mod).first;
+  }
+  *out = vit->second->kernels.at(march_kernel_name(v));
+  return LINON_OK;
 }
 
 int field_valid(const linon_ctx* ctx, const linon_field* f) {
@@ -435,7 +473,10 @@ int linon_field_validate(const char* field_body, const char* helpers_src, int fl
   }
   std::string jlog;
   size_t bytes = 0;
-  int st = jit_check(module_source(t.code), (flags & LINON_COMPILE_PRECISE) != 0, jlog, &bytes);
+  const bool precise = (flags & LINON_COMPILE_PRECISE) != 0;
+  // the reference's variant (t-loop, adaptive) and the fixed-step Kahan
+  // variant, each with and without the field_weight == 1 specialisation
+  int st = jit_check(module_source(t.code, {1, 9, 6, 14}, true), precise, jlog, &bytes);
   copy_log(jlog, log, log_cap);
   if (st != LINON_OK) return set_error(st, jlog);
   return LINON_OK;
@@ -456,7 +497,8 @@ int linon_field_compile(linon_ctx* ctx, const char* field_body, const char* help
   const bool precise = (flags & LINON_COMPILE_PRECISE) != 0;
   std::shared_ptr<JitModule> mod;
   std::string jlog;
-  int st = jit_compile(module_source(t.code), precise, module_kernels(), mod, jlog);
+  const std::vector<int> base = {base_variant(precise)};
+  int st = jit_compile(module_source(t.code, base, true), precise, module_kernels(base, true), mod, jlog);
   if (st != LINON_OK) {
     std::string msg = st == LINON_ECOMPILE ? jlog : g_last_error;
     copy_log(msg, log, log_cap);
@@ -518,9 +560,9 @@ int linon_render(linon_ctx* ctx, const linon_field* field, const linon_camera* c
   a.tile_w = 8;
   a.tile_h = 16;
   a.err = ctx->d_err;
-  const char* name = params->adaptive ? (params->kahan ? "linon_march_a1_k1" : "linon_march_a1_k0")
-                                      : (params->kahan ? "linon_march_a0_k1" : "linon_march_a0_k0");
-  cudaKernel_t k = field->mod->kernels.at(name);
+  cudaKernel_t k;
+  const bool precise = (field->flags & LINON_COMPILE_PRECISE) != 0;
+  if (int st = march_kernel(field, march_variant(params, settings, precise), &k)) return st;
   dim3 grid((out->width + a.tile_w - 1) / a.tile_w, (out->height + a.tile_h - 1) / a.tile_h);
   void* args[] = {&a};
   LINON_CUDA(cudaLaunchKernel((const void*)k, grid, dim3(a.tile_w * a.tile_h), args,

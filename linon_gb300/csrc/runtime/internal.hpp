@@ -88,7 +88,9 @@ struct linon_field {
   std::string body, helpers, cuda;
   int flags = 0;
   int flops_arith = 0, flops_transc = 0;
-  std::shared_ptr<linon::JitModule> mod;
+  std::shared_ptr<linon::JitModule> mod;  // capture, field_eval, base march variant
+  mutable std::mutex vmu;                  // guards `variants`
+  mutable std::map<int, std::shared_ptr<linon::JitModule>> variants;  // other march variants
 };
 
 struct linon_ctx {
