@@ -77,6 +77,11 @@ WG_HD void sincos_fast(float x, float* s, float* c) {
   float r = fmaf(-q, 0x1.921fb6p+0f, x);      // pi/2 = P1 + P2 + P3
   r = fmaf(-q, -0x1.777a5cp-25f, r);
   r = fmaf(-q, -0x1.ee59dap-50f, r);
+#if defined(LINON_SINCOS_SFU)
+  // the special-function unit on the reduced argument (|r| <= pi/4)
+  const float sn = __sinf(r);
+  const float cs = __cosf(r);
+#else
   const float r2 = r * r;
   float ps = fmaf(r2, 2.75573192e-6f, -1.98412698e-4f);  // 1/9!, -1/7!
   ps = fmaf(r2, ps, 8.33333333e-3f);                       // 1/5!
@@ -87,6 +92,7 @@ WG_HD void sincos_fast(float x, float* s, float* c) {
   pc = fmaf(r2, pc, 4.16666667e-2f);                       // 1/4!
   pc = fmaf(r2, pc, -0.5f);                                // -1/2!
   const float cs = fmaf(r2, pc, 1.0f);
+#endif
   const int qi = int(q) & 3;
   const float a = (qi & 1) ? cs : sn;
   const float b = (qi & 1) ? sn : cs;

@@ -58,6 +58,13 @@ std::vector<std::string> options(bool precise) {
     o.push_back("--prec-sqrt=false");
   }
   if (std::getenv("LINON_JIT_VERBOSE")) o.push_back("--ptxas-options=--verbose");
+  // extra NVRTC options (space separated), e.g. "-maxrregcount=64" or
+  // "-DLINON_SINCOS_SFU" (see wgsl_rt.cuh); they are part of the cache key
+  if (const char* extra = std::getenv("LINON_JIT_OPTIONS")) {
+    std::istringstream is(extra);
+    std::string opt;
+    while (is >> opt) o.push_back(opt);
+  }
   return o;
 }
 
