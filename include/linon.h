@@ -43,7 +43,8 @@ enum linon_status {
   LINON_ETIMEOUT = 5,  /* a bounded device- or host-side wait ran out           */
   LINON_ENOSCENE = 6,  /* render called before linon_scene_upload               */
   LINON_EBUSY = 7,     /* serving queue full / context busy                     */
-  LINON_ESTATE = 8     /* call not valid in the current state                   */
+  LINON_ESTATE = 8,    /* call not valid in the current state                   */
+  LINON_EIO = 9        /* a file could not be read                              */
 };
 
 /* ---- data ABI (byte-compatible with the reference's uniforms) ---------- */
@@ -174,6 +175,41 @@ int linon_scene_upload(linon_ctx* ctx, const float* xyz, uint32_t n_vertices,
 /* BVH statistics of the current scene: nodes, leaves, max depth.          */
 int linon_scene_info(const linon_ctx* ctx, uint32_t* n_faces, uint32_t* n_nodes,
                      uint32_t* max_depth);
+
+/* ---- OBJ ingestion: replaces the dropped-file path, src/main.rs:139-156
+ * (tobj 4.0.2 `load_obj` with triangulate = true, models[0].mesh) and
+ * Application::load_model (src/application.rs:199-226).
+ * Positions come in the order of their first reference by a face of the
+ * model (tobj's default multi-index export); faces are triangles (quads and
+ * polygons as fans around their first vertex, points and lines as
+ * zero-area triangles).  `model` selects tobj's models[model]: files are
+ * split into models at "o" / "g" records and at "usemtl" switches between
+ * materials named in the "mtllib" files.  LINON_OBJ_NORMALIZE applies
+ * normalize_vertices (src/vertices.rs:3-17) as load_model does; the
+ * reported centre is get_center (src/vertices.rs:19-57) of the returned
+ * positions.  Errors: LINON_EIO (file unreadable), LINON_EINVAL with
+ * "obj line N: ..." (malformed record, index out of range, no such model);
+ * *out is NULL then.  The mesh is host memory owned by the caller.        */
+typedef struct linon_mesh linon_mesh;
+#define LINON_OBJ_NORMALIZE 1u
+int linon_obj_load(const char* path, uint32_t model, uint32_t flags, linon_mesh** out);
+/* The same from text in memory; "mtllib" files are looked up in mtl_dir
+ * (NULL: no material file is read and every material name is unknown).    */
+int linon_obj_parse(const char* text, size_t len, const char* mtl_dir, uint32_t model,
+                    uint32_t flags, linon_mesh** out);
+/* Vertex / triangle counts, the number of models in the file and the
+ * bounding-box centre of the returned positions (any pointer may be NULL). */
+int linon_mesh_info(const linon_mesh* mesh, uint32_t* n_vertices, uint32_t* n_faces,
+                    uint32_t* n_models, float center[3]);
+const float* linon_mesh_positions(const linon_mesh* mesh); /* n_vertices*3 */
+const uint32_t* linon_mesh_faces(const linon_mesh* mesh);  /* n_faces*3    */
+void linon_mesh_free(linon_mesh* mesh);
+/* normalize_vertices (src/vertices.rs:3-17) in place over n_floats
+ * coordinates: one min and max over all of them, x' = (x-min)/(max-min)*2-1
+ * in f32; then get_center (src/vertices.rs:19-57) into center (may be NULL;
+ * needs n_floats >= 3).  Equal min and max give non-finite results, as in
+ * the reference.                                                          */
+int linon_normalize_vertices(float* xyz, size_t n_floats, float center[3]);
 
 /* ---- field functions: replaces MainView::reload_shader
  *      (main_view.rs:649-690) and with_field_function (main_view.rs:852-861)

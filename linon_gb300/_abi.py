@@ -21,6 +21,8 @@ LINON_ETIMEOUT = 5
 LINON_ENOSCENE = 6
 LINON_EBUSY = 7
 LINON_ESTATE = 8
+LINON_EIO = 9
+LINON_OBJ_NORMALIZE = 1
 LINON_COMPILE_PRECISE = 1
 LINON_MAX_BATCH_FIELDS = 8
 
@@ -120,6 +122,13 @@ PROTOTYPES = {
     "linon_device_bytes": (sz, [vp]),
     "linon_scene_upload": (C.c_int, [vp, vp, C.c_uint32, vp, C.c_uint32, vp, C.c_int]),
     "linon_scene_info": (C.c_int, [vp, P(C.c_uint32), P(C.c_uint32), P(C.c_uint32)]),
+    "linon_obj_load": (C.c_int, [C.c_char_p, C.c_uint32, C.c_uint32, P(vp)]),
+    "linon_obj_parse": (C.c_int, [C.c_char_p, sz, C.c_char_p, C.c_uint32, C.c_uint32, P(vp)]),
+    "linon_mesh_info": (C.c_int, [vp, P(C.c_uint32), P(C.c_uint32), P(C.c_uint32), P(C.c_float)]),
+    "linon_mesh_positions": (P(C.c_float), [vp]),
+    "linon_mesh_faces": (P(C.c_uint32), [vp]),
+    "linon_mesh_free": (None, [vp]),
+    "linon_normalize_vertices": (C.c_int, [vp, sz, P(C.c_float)]),
     "linon_field_compile": (C.c_int, [vp, cp, cp, C.c_int, P(vp), C.c_char_p, sz]),
     "linon_field_release": (C.c_int, [vp, vp]),
     "linon_field_flops": (C.c_int, [vp, P(i32), P(i32)]),

@@ -37,6 +37,7 @@ CPP_SOURCES = [
     "runtime/api.cpp",
     "runtime/batch.cpp",
     "runtime/serve.cpp",
+    "runtime/obj.cpp",
 ]
 CU_SOURCES = ["runtime/kernels.cu", "runtime/noalloc.cu"]
 GENERATED = BUILD_DIR / "embedded_sources.cpp"

@@ -33,16 +33,6 @@ int cuda_error(cudaError_t e, const char* what) {
 
 namespace {
 
-#define LINON_TRY_BEGIN try {
-#define LINON_TRY_END                                                          \
-  }                                                                            \
-  catch (const std::bad_alloc&) {                                              \
-    return set_error(LINON_ENOMEM, "host allocation failed");                  \
-  }                                                                            \
-  catch (const std::exception& ex) {                                           \
-    return set_error(LINON_EINVAL, std::string("internal error: ") + ex.what()); \
-  }
-
 int dev_alloc(linon_ctx* ctx, DevBuf& b, size_t bytes) {
   if (b.bytes >= bytes && b.p) return LINON_OK;
   size_t grow = bytes - b.bytes;
@@ -306,6 +296,7 @@ const char* linon_status_string(int status) {
     case LINON_ENOSCENE: return "no scene uploaded";
     case LINON_EBUSY: return "busy";
     case LINON_ESTATE: return "invalid state";
+    case LINON_EIO: return "file could not be read";
   }
   return "unknown status";
 }

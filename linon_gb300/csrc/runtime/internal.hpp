@@ -24,6 +24,17 @@ int cuda_error(cudaError_t e, const char* what);
     if (e_ != cudaSuccess) return ::linon::cuda_error(e_, #call); \
   } while (0)
 
+// no exception crosses the C ABI: entry points wrap their bodies in these
+#define LINON_TRY_BEGIN try {
+#define LINON_TRY_END                                                                       \
+  }                                                                                         \
+  catch (const std::bad_alloc&) {                                                           \
+    return ::linon::set_error(LINON_ENOMEM, "host allocation failed");                      \
+  }                                                                                         \
+  catch (const std::exception& ex) {                                                        \
+    return ::linon::set_error(LINON_EINVAL, std::string("internal error: ") + ex.what());    \
+  }
+
 // ---- device memory owned by a context -----------------------------------
 struct DevBuf {
   void* p = nullptr;

@@ -69,6 +69,15 @@ class MainView:
         self.camera.zoom(-1.0, 1.0)
         self.update_camera()
 
+    def load_obj(self, path, model: int = 0):
+        """A dropped .obj file (src/main.rs:139-156): tobj's models[model]
+        with triangulation, normalize_vertices and get_center
+        (src/application.rs:199-226), then update_model.  Returns the mesh."""
+        from . import scene
+        mesh = scene.load_obj(path, model=model, normalize=True)
+        self.update_model(mesh.xyz, mesh.faces, mesh.center)
+        return mesh
+
     def update_settings(self, settings: _abi.Settings):
         self.settings = settings
         self.needs_redraw = True

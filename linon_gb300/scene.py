@@ -171,3 +171,93 @@ def cornell_with_spheres(seed: int = 0, n: int = 4, subdivisions: int = 5, radiu
         x, f = icosphere(subdivisions, radius, c)
         meshes.append((x, f, np.full((len(f), 3), (0.9, 0.9, 0.95), np.float32)))
     return merge(*meshes)
+
+
+# ---- OBJ ingestion (src/main.rs:139-156, src/application.rs:199-226) ----
+
+class ObjMesh:
+    """One model of an OBJ file as the native loader returns it: positions
+    (float32 [n,3]) in first-reference order, triangles (uint32 [m,3]), the
+    number of models in the file and the bounding-box centre."""
+
+    def __init__(self, xyz, faces, center, n_models):
+        self.xyz, self.faces, self.center, self.n_models = xyz, faces, center, n_models
+
+
+def _mesh_from_handle(lib, h) -> ObjMesh:
+    import ctypes as C
+    try:
+        nv, nf, nm = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        c = (C.c_float * 3)()
+        lib.linon_mesh_info(h, C.byref(nv), C.byref(nf), C.byref(nm), c)
+        xyz = np.ctypeslib.as_array(lib.linon_mesh_positions(h), (nv.value * 3,)).copy() if nv.value else \
+            np.zeros(0, np.float32)
+        faces = np.ctypeslib.as_array(lib.linon_mesh_faces(h), (nf.value * 3,)).copy() if nf.value else \
+            np.zeros(0, np.uint32)
+        return ObjMesh(xyz.reshape(-1, 3), faces.reshape(-1, 3), np.array(c[:], np.float32), nm.value)
+    finally:
+        lib.linon_mesh_free(h)
+
+
+def load_obj(path, model: int = 0, normalize: bool = True) -> ObjMesh:
+    """The reference's dropped-file path: tobj's load_obj with triangulation,
+    models[model].mesh, then (normalize=True) load_model's normalize_vertices
+    and get_center.  Raises LinonError on unreadable or malformed files."""
+    import ctypes as C
+    from . import _abi
+    lib = _abi.load()
+    h = C.c_void_p()
+    _abi.check(lib.linon_obj_load(str(path).encode(), model, _abi.LINON_OBJ_NORMALIZE if normalize else 0,
+                                  C.byref(h)))
+    return _mesh_from_handle(lib, h)
+
+
+def parse_obj(text, model: int = 0, normalize: bool = True, mtl_dir=None) -> ObjMesh:
+    """load_obj on OBJ text in memory ("mtllib" files are read from mtl_dir)."""
+    import ctypes as C
+    from . import _abi
+    lib = _abi.load()
+    data = text.encode() if isinstance(text, str) else bytes(text)
+    h = C.c_void_p()
+    _abi.check(lib.linon_obj_parse(data, len(data), None if mtl_dir is None else str(mtl_dir).encode(), model,
+                                   _abi.LINON_OBJ_NORMALIZE if normalize else 0, C.byref(h)))
+    return _mesh_from_handle(lib, h)
+
+
+def normalize_vertices_native(xyz) -> tuple[np.ndarray, np.ndarray]:
+    """normalize_vertices + get_center through the C ABI (float32, in place on a copy)."""
+    import ctypes as C
+    from . import _abi
+    v = np.ascontiguousarray(xyz, dtype=np.float32).copy()
+    c = (C.c_float * 3)()
+    _abi.check(_abi.load().linon_normalize_vertices(v.ctypes.data, v.size, c if v.size >= 3 else None))
+    return v, np.array(c[:], np.float32)
+
+
+def to_obj(xyz, faces, polygons=None) -> str:
+    """OBJ text of a triangle mesh ("v" and 1-based "f" records); extra
+    polygons (lists of 0-based vertex indices) are appended as faces."""
+    xyz = np.asarray(xyz, np.float32).reshape(-1, 3)
+    lines = [f"v {float(a)!r} {float(b)!r} {float(c)!r}" for a, b, c in xyz.tolist()]
+    lines += [f"f {a + 1} {b + 1} {c + 1}" for a, b, c in np.asarray(faces).reshape(-1, 3).tolist()]
+    for poly in polygons or []:
+        lines.append("f " + " ".join(str(i + 1) for i in poly))
+    return "\n".join(lines) + "\n"
+
+
+def torus(n_major: int = 48, n_minor: int = 24, R: float = 0.35, r: float = 0.12, center=(0.0, 0.0, 0.0),
+          tilt: float = 0.6):
+    """Torus as quads (for OBJ files with non-triangle faces): vertices
+    float32 [n_major*n_minor, 3] and quads int [n_major*n_minor, 4], tilted
+    about the x axis by `tilt` radians."""
+    i, j = np.meshgrid(np.arange(n_major), np.arange(n_minor), indexing="ij")
+    u, v = 2 * np.pi * i / n_major, 2 * np.pi * j / n_minor
+    x = (R + r * np.cos(v)) * np.cos(u)
+    y = (R + r * np.cos(v)) * np.sin(u)
+    z = r * np.sin(v)
+    ct, st = np.cos(tilt), np.sin(tilt)
+    y, z = y * ct - z * st, y * st + z * ct
+    xyz = np.stack([x, y, z], -1).reshape(-1, 3) + np.asarray(center)
+    idx = lambda a, b: (a % n_major) * n_minor + (b % n_minor)
+    quads = np.stack([idx(i, j), idx(i + 1, j), idx(i + 1, j + 1), idx(i, j + 1)], -1).reshape(-1, 4)
+    return xyz.astype(np.float32), quads

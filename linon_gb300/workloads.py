@@ -10,6 +10,10 @@
   batch_uneven (64 seeded views, 128^2..1024^2 log-uniform, cameras on the
   radius-3 sphere, h in {0.02, 0.01, 0.005}, 4/h steps, Cornell room + four
   20,480-triangle icospheres behind the BVH, stop at the first hit).
+* obj_scene: an OBJ file (raw Cornell box triangles, a quad torus, a hexagon
+  and a pentagon) loaded the way a dropped file is (tobj triangulation,
+  normalize_vertices, get_center, arcball default camera), the shader's own
+  loop.
 """
 from __future__ import annotations
 
@@ -109,3 +113,38 @@ def batch_uneven(n_views=64, seed=0) -> Workload:
                  [_abi.FIELD_IDS["linear"], _abi.FIELD_IDS["twist"], _abi.FIELD_IDS["lens"]])
     w.extra["views"] = batch_views(n_views, seed)
     return w
+
+
+def obj_scene_text() -> str:
+    """OBJ text of the obj_scene workload: the raw Cornell box (triangles),
+    a tilted quad torus inside it, a hexagon on the back wall and a pentagon
+    on the floor (fans); two models: "o cornell" and "g torus" (torus,
+    hexagon, pentagon), plus a trailing empty object."""
+    v, f, _ = scene.cornell_raw()
+    tv, tq = scene.torus(center=(278.0, 200.0, 280.0), R=120.0, r=40.0)
+    lines = ["# obj_scene: Cornell box, torus, hexagon, pentagon", "o cornell"]
+    lines += [f"v {a!r} {b!r} {c!r}" for a, b, c in v.astype(float).tolist()]
+    lines += [f"f {a + 1} {b + 1} {c + 1}" for a, b, c in f.tolist()]
+    lines.append("g torus")
+    lines += [f"v {a!r} {b!r} {c!r}" for a, b, c in tv.astype(float).tolist()]
+    lines += ["f " + " ".join(f"{-(len(tv) - k)}" for k in q) for q in tq.tolist()]  # relative indices
+    ang = np.arange(6) * np.pi / 3
+    hexv = np.stack([278 + 60 * np.cos(ang), 380 + 60 * np.sin(ang), np.full(6, 555.0)], -1)
+    lines += [f"v {a!r} {b!r} {c!r}" for a, b, c in hexv.tolist()]
+    lines.append("f " + " ".join(str(-6 + k) for k in range(6)))
+    ang5 = np.arange(5) * 2 * np.pi / 5
+    pentv = np.stack([150 + 50 * np.cos(ang5), np.full(5, 0.5), 420 + 50 * np.sin(ang5)], -1)
+    lines += [f"v {a!r} {b!r} {c!r}" for a, b, c in pentv.tolist()]
+    lines.append("f " + " ".join(str(-5 + k) for k in range(5)))
+    lines.append("o trailing_empty")
+    return "\n".join(lines) + "\n"
+
+
+def obj_scene(width=256, height=192, model: int = 0, text: str | None = None) -> Workload:
+    """The OBJ scene as the reference's dropped-file path loads it: the first
+    model (\"o cornell\" ends at \"g torus\", so model 0 is the box alone;
+    model=1 is the torus with the two panels)."""
+    m = scene.parse_obj(text or obj_scene_text(), model=model, normalize=True)
+    return Workload(f"obj_scene_model{model}_{width}x{height}", m.xyz, m.faces, None, width, height,
+                    cam.arcball_default(m.center), settings(), _abi.reference_params(),
+                    [_abi.FIELD_IDS["mirage_spherical_sigmoid"]], extra={"n_models": m.n_models})
