@@ -62,30 +62,35 @@ WG_HD unsigned to_u32(int x) { return unsigned(x); }
 WG_HD unsigned to_u32(unsigned x) { return x; }
 
 // Sine and cosine of one argument with one range reduction (fast modules).
-// Method: Cody & Waite's additive reduction x = q * pi/2 + r with pi/2 split
-// into three floats (each product applied by an FMA), then sin(r), cos(r) on
-// |r| <= pi/4 from the special-function unit (or, with LINON_SINCOS_POLY, the
-// Taylor series of sin to r^9 and of cos to r^10: truncation below 2.5e-9
-// relative), and the quadrant's swap and signs.  |x| >= 65536 (and inf/NaN)
-// take the CUDA library's sincosf.
+// Method: Cody & Waite's additive reduction x = k * P + r, the period split
+// into three floats (pi/2 = P1 + P2 + P3, each product applied by an FMA).
+// Default: P = 2 pi (the split scaled by 4, exact) and sin(r), cos(r) on
+// |r| <= pi from the special-function unit, whose documented absolute error
+// there is 2^-21.41; the reduced argument's own rounding adds at most half an
+// ulp of pi, so the result is within 5e-7 of sin/cos of the float argument,
+// and no quadrant bookkeeping is needed.  With LINON_SINCOS_POLY: P = pi/2,
+// the Taylor series of sin to r^9 and of cos to r^10 on |r| <= pi/4
+// (truncation below 2.5e-9 relative), and the quadrant's swap and signs
+// (error below 2.5e-7).  |x| >= 65536 (and inf/NaN) take the CUDA library's
+// sincosf.
 WG_HD void sincos_fast(float x, float* s, float* c) {
 #if defined(__CUDA_ARCH__)
   if (!(fabsf(x) < 65536.0f)) {
     sincosf(x, s, c);
     return;
   }
+#if !defined(LINON_SINCOS_POLY)
+  const float k = rintf(x * 0x1.45f306p-3f);  // x / (2 pi)
+  float r = fmaf(-k, 0x1.921fb6p+2f, x);      // 2 pi = 4 (P1 + P2 + P3)
+  r = fmaf(-k, -0x1.777a5cp-23f, r);
+  r = fmaf(-k, -0x1.ee59dap-48f, r);
+  *s = __sinf(r);
+  *c = __cosf(r);
+#else
   const float q = rintf(x * 0x1.45f306p-1f);  // x * 2/pi
   float r = fmaf(-q, 0x1.921fb6p+0f, x);      // pi/2 = P1 + P2 + P3
   r = fmaf(-q, -0x1.777a5cp-25f, r);
   r = fmaf(-q, -0x1.ee59dap-50f, r);
-#if !defined(LINON_SINCOS_POLY)
-  // the special-function unit on the reduced argument (|r| <= pi/4):
-  // absolute error below 4e-7 (measured against FP64), 14% faster twist
-  // frames than the polynomials below (which stay available with
-  // -DLINON_SINCOS_POLY, error below 2.5e-7)
-  const float sn = __sinf(r);
-  const float cs = __cosf(r);
-#else
   const float r2 = r * r;
   float ps = fmaf(r2, 2.75573192e-6f, -1.98412698e-4f);  // 1/9!, -1/7!
   ps = fmaf(r2, ps, 8.33333333e-3f);                       // 1/5!
@@ -96,12 +101,12 @@ WG_HD void sincos_fast(float x, float* s, float* c) {
   pc = fmaf(r2, pc, 4.16666667e-2f);                       // 1/4!
   pc = fmaf(r2, pc, -0.5f);                                // -1/2!
   const float cs = fmaf(r2, pc, 1.0f);
-#endif
   const int qi = int(q) & 3;
   const float a = (qi & 1) ? cs : sn;
   const float b = (qi & 1) ? sn : cs;
   *s = (qi & 2) ? -a : a;
   *c = ((qi + 1) & 2) ? -b : b;
+#endif
 #else
   *s = sinf(x);
   *c = cosf(x);

@@ -91,6 +91,40 @@ def test_precise_transcendental_fields_close(engine, oracle, name):
     assert np.percentile(d[same], 99) <= tol
 
 
+@pytest.mark.parametrize("precise", [True, False])
+def test_reference_default_frame(engine, oracle, precise):
+    """The reference application's first frame: the Cornell box as
+    application.rs prepares it, the arcball default camera, the spherical
+    sigmoid mirage field, the shader's t <= 5 loop (h = 0.1, adaptive), at
+    200x150.
+
+    The shader's refinement test (diff > 10 * last_diff) compares velocity
+    changes that, away from the heated region, are rounding noise: the FP32
+    and FP64 oracles agree on the step count of only ~0.2% of these pixels
+    (median 82 vs 1342 steps) while agreeing on 99.8% of hit ids.  Step counts
+    are therefore held exactly only for the precise module (op-for-op the
+    FP32 oracle; exp differs in the last bit, so >= 98% of pixels); the fast
+    module (FMA) is held to what survives rounding: hit ids on >= 98% of
+    pixels and endpoints within 0.12 at the 99th percentile: one coarse step
+    (0.1, the spread of the last step past t = 5) plus 20%; the FP32 and FP64
+    oracles differ by 0.084 there."""
+    w = wl.reference_default(200, 150)
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    g = gpu_render(engine, w, field(engine, "mirage_spherical_sigmoid", precise))
+    o = oracle_render(oracle, w, _abi.FIELD_IDS["mirage_spherical_sigmoid"], w.width, w.height)
+    hit_ok = np.mean(g["hit_id"] == o["hit_id"])
+    assert hit_ok >= (0.99 if precise else 0.98), hit_ok
+    d = np.abs(g["mapping"][..., :3] - o["mapping"][..., :3]).max(axis=-1)
+    if precise:
+        steps_ok = np.mean(g["steps"] == o["steps"])
+        assert steps_ok >= 0.98, steps_ok
+        same = (g["steps"] == o["steps"]) & (g["hit_id"] == o["hit_id"])
+        assert np.percentile(d[same], 99) <= 1e-4
+    else:
+        assert np.percentile(d, 99) <= 0.12, np.percentile(d, 99)
+    assert (o["steps"] >= 51).all() and (g["steps"] >= 51).all()  # t <= 5 at h <= 0.1
+
+
 @pytest.mark.parametrize("name", ["linear", "twist", "lens"])
 def test_fast_vs_fp64_1080p(engine, oracle, name):
     """The 1080p workload (h = 0.005, 4000 steps, Kahan sums), fast module,
@@ -124,8 +158,10 @@ def test_fast_vs_fp64_1080p(engine, oracle, name):
 
 
 def test_fast_math_accuracy(engine):
-    """Fast modules' sin/cos (one Cody-Waite reduction + Taylor polynomials)
-    and constant-exponent pow against FP64."""
+    """Fast modules' sin/cos (one Cody-Waite reduction by 2 pi, then the
+    special-function unit on |r| <= pi: its documented 2^-21.41 plus half an
+    ulp of pi from the reduced argument, < 5e-7 absolute) and
+    constant-exponent pow against FP64."""
     body = "return vec3<f32>(sin(t), cos(t), pow(p.x, 1.5));"
     fld = engine.compile_field(body)
     n = 1 << 18
@@ -135,9 +171,8 @@ def test_fast_math_accuracy(engine):
     x[:, 3] = rng.uniform(0, 50, n).astype(np.float32)
     out = engine.field_eval(fld, torch.from_numpy(x).cuda()).cpu().numpy().astype(np.float64)
     t = x[:, 12].astype(np.float64)
-    # special-function unit on the Cody-Waite-reduced argument: < 4e-7 absolute
-    assert np.abs(out[:, 0] - np.sin(t)).max() <= 4e-7
-    assert np.abs(out[:, 1] - np.cos(t)).max() <= 4e-7
+    assert np.abs(out[:, 0] - np.sin(t)).max() <= 5e-7
+    assert np.abs(out[:, 1] - np.cos(t)).max() <= 5e-7
     ref = x[:, 3].astype(np.float64) ** 1.5
     assert (np.abs(out[:, 2] - ref) / np.maximum(ref, 1e-30)).max() <= 3.6e-7
 
