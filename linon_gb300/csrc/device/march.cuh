@@ -101,6 +101,16 @@ __device__ __forceinline__ bool box_overlap(const float4& lo, const float4& hi, 
 #define LINON_BVH_STACK 48
 #endif
 
+// Launch bounds of the plain march kernels (128-thread CTAs).  Defining
+// LINON_MARCH_MIN_CTAS adds the minimum resident CTAs per SM, which caps the
+// registers per thread (and may spill).
+#ifdef LINON_MARCH_MIN_CTAS
+#define LINON_MARCH_BOUNDS __launch_bounds__(128, LINON_MARCH_MIN_CTAS)
+#else
+#define LINON_MARCH_BOUNDS __launch_bounds__(128)
+#endif
+
+
 // Segment query; seg_end is origin + step (the unnormalised step vector).
 __device__ __forceinline__ HitRec intersect_segment(const SceneView& sc, const vec3f& origin,
                                                     const vec3f& direction, float max_dist,
@@ -220,7 +230,18 @@ __device__ __forceinline__ wgsl::vec4f shade_hit(const SceneView& sc, const HitR
   vec3f normal = wgsl::normalize(wgsl::cross(d1, d2));
   float intensity = wgsl::max(wgsl::dot(normal, -direction), 0.0f);
   if (intensity == 0.0f) intensity = wgsl::max(wgsl::dot(-normal, -direction), 0.0f);
+#if defined(LINON_PRECISE)
   float spec = powf(intensity, 64.0f);
+#else
+  // x^64 by six squarings (fast modules): a few ulp from powf, and far less
+  // code in the march loop than the library pow
+  float spec = intensity * intensity;
+  spec *= spec;
+  spec *= spec;
+  spec *= spec;
+  spec *= spec;
+  spec *= spec;
+#endif
   float shade = (0.01f + intensity) + spec;
   vec3f base = wgsl::abs(normal);
   if (sc.face_rgb) {
@@ -565,6 +586,24 @@ __device__ __forceinline__ void march_plain_kernel(const F& field, const MarchAr
     if (a.frame.steps) a.frame.steps[idx] = 0;
     return;
   }
+#if !defined(LINON_VOTE_LOOP)
+  if ((V & V_STEPS) && !ADAPTIVE && !a.m.stop_on_hit) {
+    // Fixed step budget without adaptive retries or early stop: every lane
+    // takes exactly max_steps steps (lanes outside the image march pixel
+    // (0, 0)'s ray and store nothing), so the trip count is the same for the
+    // whole warp and no vote is needed; __syncwarp after each step
+    // reconverges lanes that diverged at an intersection test.
+    // One copy of the step in the loop: the step inlines the BVH traversal,
+    // and a second copy (unrolling, a remainder loop) costs more in
+    // instruction-cache misses than it saves.
+    for (int s = 0; s < a.m.max_steps; ++s) {
+      ray_step<ADAPTIVE, KAHAN, W1>(r, field, a.m, sc, a.err);
+      __syncwarp();
+    }
+    if (in_image) ray_store(r, a.frame, idx);
+    return;
+  }
+#endif
   // The vote at the top of every step reconverges the warp: without it the
   // lanes that diverged at a (rare) intersection test would walk the rest of
   // the march separately, a few lanes per issued instruction.

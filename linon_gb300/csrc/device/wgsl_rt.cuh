@@ -64,21 +64,19 @@ WG_HD unsigned to_u32(unsigned x) { return x; }
 // Sine and cosine of one argument with one range reduction (fast modules).
 // Method: Cody & Waite's additive reduction x = k * P + r, the period split
 // into three floats (pi/2 = P1 + P2 + P3, each product applied by an FMA).
-// Default: P = 2 pi (the split scaled by 4, exact) and sin(r), cos(r) on
-// |r| <= pi from the special-function unit, whose documented absolute error
-// there is 2^-21.41; the reduced argument's own rounding adds at most half an
-// ulp of pi, so the result is within 5e-7 of sin/cos of the float argument,
-// and no quadrant bookkeeping is needed.  With LINON_SINCOS_POLY: P = pi/2,
+// Default: P = 2 pi (the split scaled by 4, exact) and sin(r), cos(r) from
+// the special-function unit, whose documented absolute error on [-pi, pi]
+// is 2^-21.41; the reduced argument is within 1.3e-7 of the exact
+// x - k * 2 pi for |x| < 2^22.  Measured against FP64: < 5e-7 for
+// |x| <= 3000, < 1e-6 for |x| < 2^22 (there the rounding of x / (2 pi) can
+// leave |r| a little above pi); beyond, the error grows with |x|, like the
+// special-function unit's own; inf and NaN give NaN.  No quadrant
+// bookkeeping or range branch is needed.  With LINON_SINCOS_POLY: P = pi/2,
 // the Taylor series of sin to r^9 and of cos to r^10 on |r| <= pi/4
-// (truncation below 2.5e-9 relative), and the quadrant's swap and signs
-// (error below 2.5e-7).  |x| >= 65536 (and inf/NaN) take the CUDA library's
-// sincosf.
+// (truncation below 2.5e-9 relative) and the quadrant's swap and signs
+// (error below 2.5e-7); |x| >= 65536 takes the CUDA library's sincosf.
 WG_HD void sincos_fast(float x, float* s, float* c) {
 #if defined(__CUDA_ARCH__)
-  if (!(fabsf(x) < 65536.0f)) {
-    sincosf(x, s, c);
-    return;
-  }
 #if !defined(LINON_SINCOS_POLY)
   const float k = rintf(x * 0x1.45f306p-3f);  // x / (2 pi)
   float r = fmaf(-k, 0x1.921fb6p+2f, x);      // 2 pi = 4 (P1 + P2 + P3)
@@ -87,6 +85,10 @@ WG_HD void sincos_fast(float x, float* s, float* c) {
   *s = __sinf(r);
   *c = __cosf(r);
 #else
+  if (!(fabsf(x) < 65536.0f)) {
+    sincosf(x, s, c);
+    return;
+  }
   const float q = rintf(x * 0x1.45f306p-1f);  // x * 2/pi
   float r = fmaf(-q, 0x1.921fb6p+0f, x);      // pi/2 = P1 + P2 + P3
   r = fmaf(-q, -0x1.777a5cp-25f, r);
@@ -207,6 +209,50 @@ template <class T> struct vec<T, 4> {
   WG_HD T& operator[](int i) { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
   WG_HD T operator[](int i) const { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
 };
+
+// array<T, N>: value semantics (copied on assignment and by value into
+// functions), zero-initialised by default; a runtime index is clamped to
+// [0, N-1] (wgpu's default bounds-check policy).
+template <class T, int N>
+struct arr {
+  T v[N];
+  WG_HD arr() : v{} {}
+  template <class... A>
+  WG_HD explicit arr(const T& a0, const A&... a) : v{a0, T(a)...} {
+    static_assert(sizeof...(A) + 1 == N, "array constructor with the wrong number of elements");
+  }
+  WG_HD T& operator[](int i) { return v[i < 0 ? 0 : (i >= N ? N - 1 : i)]; }
+  WG_HD const T& operator[](int i) const { return v[i < 0 ? 0 : (i >= N ? N - 1 : i)]; }
+  WG_HD T& operator[](unsigned i) { return v[i >= unsigned(N) ? unsigned(N - 1) : i]; }
+  WG_HD const T& operator[](unsigned i) const { return v[i >= unsigned(N) ? unsigned(N - 1) : i]; }
+};
+
+// bitcast<T>(e): the bits of a 32-bit scalar (or of each vector component)
+// reinterpreted as another 32-bit scalar type.
+template <class To, class From>
+struct Bitcast {
+  static WG_HD To go(const From& x) {
+    static_assert(sizeof(To) == 4 && sizeof(From) == 4, "bitcast of 32-bit types");
+    union {
+      From f;
+      To t;
+    } c;
+    c.f = x;
+    return c.t;
+  }
+};
+template <class To, class From, int N>
+struct Bitcast<vec<To, N>, vec<From, N>> {
+  static WG_HD vec<To, N> go(const vec<From, N>& x) {
+    vec<To, N> r;
+    for (int i = 0; i < N; ++i) r[i] = Bitcast<To, From>::go(x[i]);
+    return r;
+  }
+};
+template <class To, class From>
+WG_HD To bitcast_(const From& x) {
+  return Bitcast<To, From>::go(x);
+}
 
 typedef vec<float, 2> vec2f;
 typedef vec<float, 3> vec3f;

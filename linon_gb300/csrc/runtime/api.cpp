@@ -163,7 +163,7 @@ struct LinonField {
 };
 )LINON";
   for (int v : variants)
-    s << "extern \"C\" __global__ void __launch_bounds__(128) " << march_kernel_name(v)
+    s << "extern \"C\" __global__ void LINON_MARCH_BOUNDS " << march_kernel_name(v)
       << "(linon::MarchArgs a) {\n  linon::march_plain_kernel<" << v << ">(LinonField(), a);\n}\n";
   if (base)
     s << R"LINON(extern "C" __global__ void __launch_bounds__(256) linon_capture(linon::CaptureArgs a) {

@@ -159,20 +159,25 @@ def test_fast_vs_fp64_1080p(engine, oracle, name):
 
 def test_fast_math_accuracy(engine):
     """Fast modules' sin/cos (one Cody-Waite reduction by 2 pi, then the
-    special-function unit on |r| <= pi: its documented 2^-21.41 plus half an
-    ulp of pi from the reduced argument, < 5e-7 absolute) and
-    constant-exponent pow against FP64."""
+    special-function unit on r = x - k 2 pi) and constant-exponent pow
+    against FP64.  Bars: < 5e-7 absolute for |t| <= 3000 (the unit's
+    documented 2^-21.41 on [-pi, pi] plus the reduced argument's 1.3e-7);
+    < 1e-6 for |t| < 2^22, where the rounding of t / (2 pi) can leave |r| a
+    little above pi, outside the unit's most accurate range."""
     body = "return vec3<f32>(sin(t), cos(t), pow(p.x, 1.5));"
     fld = engine.compile_field(body)
     n = 1 << 18
     rng = np.random.default_rng(2)
     x = np.zeros((n, 13), np.float32)
-    x[:, 12] = np.concatenate([rng.uniform(-4, 4, n // 2), rng.uniform(-3000, 3000, n // 2)]).astype(np.float32)
+    small = n // 2 + n // 4
+    x[:, 12] = np.concatenate([rng.uniform(-4, 4, n // 2), rng.uniform(-3000, 3000, n // 4),
+                               rng.uniform(-4.0e6, 4.0e6, n // 4)]).astype(np.float32)
     x[:, 3] = rng.uniform(0, 50, n).astype(np.float32)
     out = engine.field_eval(fld, torch.from_numpy(x).cuda()).cpu().numpy().astype(np.float64)
     t = x[:, 12].astype(np.float64)
-    assert np.abs(out[:, 0] - np.sin(t)).max() <= 5e-7
-    assert np.abs(out[:, 1] - np.cos(t)).max() <= 5e-7
+    es, ec = np.abs(out[:, 0] - np.sin(t)), np.abs(out[:, 1] - np.cos(t))
+    assert es[:small].max() <= 5e-7 and ec[:small].max() <= 5e-7, (es[:small].max(), ec[:small].max())
+    assert es.max() <= 1e-6 and ec.max() <= 1e-6, (es.max(), ec.max())
     ref = x[:, 3].astype(np.float64) ** 1.5
     assert (np.abs(out[:, 2] - ref) / np.maximum(ref, 1e-30)).max() <= 3.6e-7
 
