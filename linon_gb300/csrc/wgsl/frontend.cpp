@@ -19,6 +19,7 @@
 #include <functional>
 #include <map>
 #include <memory>
+#include <cstdint>
 #include <set>
 #include <sstream>
 #include <stdexcept>
@@ -35,19 +36,54 @@ namespace {
 enum class SK { Bool, I32, U32, F32, AInt, AFloat };
 
 struct Ty {
-  enum Cat { Void, Scalar, Vec, Mat } cat = Void;
+  enum Cat { Void, Scalar, Vec, Mat, Arr, Struct } cat = Void;
   SK s = SK::F32;
-  int n = 0;  // vector size / matrix columns
-  int r = 0;  // matrix rows
+  int n = 0;  // vector size / matrix columns (of the element, for arrays)
+  int r = 0;  // matrix rows (of the element, for arrays)
+  // arrays: fixed-size array<E, alen> of scalar, vector, matrix or struct
+  // elements
+  Cat ecat = Void;
+  int alen = 0;
+  int sid = -1;  // struct (or array-of-struct element) index
 };
+
+// Struct declarations of the module being translated (one translation per
+// thread at a time).
+struct StructDef {
+  std::string name;
+  int line = 0, col = 0;
+  std::vector<std::pair<std::string, Ty>> members;
+};
+thread_local std::vector<StructDef>* g_structs = nullptr;
+int struct_id(const std::string& n) {
+  if (!g_structs) return -1;
+  for (size_t i = 0; i < g_structs->size(); ++i)
+    if ((*g_structs)[i].name == n) return int(i);
+  return -1;
+}
 
 Ty scalar(SK s) { Ty t; t.cat = Ty::Scalar; t.s = s; return t; }
 Ty vecT(SK s, int n) { Ty t; t.cat = Ty::Vec; t.s = s; t.n = n; return t; }
 Ty matT(int c, int r) { Ty t; t.cat = Ty::Mat; t.s = SK::F32; t.n = c; t.r = r; return t; }
 Ty voidT() { return Ty(); }
+Ty arrT(const Ty& el, int len) {
+  Ty t = el;
+  t.ecat = el.cat;
+  t.cat = Ty::Arr;
+  t.alen = len;
+  return t;
+}
+Ty elemT(const Ty& a) {
+  Ty t = a;
+  t.cat = a.ecat;
+  t.ecat = Ty::Void;
+  t.alen = 0;
+  return t;
+}
 
 bool operator==(const Ty& a, const Ty& b) {
-  return a.cat == b.cat && (a.cat == Ty::Void || (a.s == b.s && a.n == b.n && a.r == b.r));
+  return a.cat == b.cat && (a.cat == Ty::Void || (a.s == b.s && a.n == b.n && a.r == b.r && a.ecat == b.ecat &&
+                                                  a.alen == b.alen && a.sid == b.sid));
 }
 bool operator!=(const Ty& a, const Ty& b) { return !(a == b); }
 
@@ -73,6 +109,8 @@ std::string wgsl_name(const Ty& t) {
     case Ty::Scalar: return sk_name(t.s);
     case Ty::Vec: return "vec" + std::to_string(t.n) + "<" + sk_name(t.s) + ">";
     case Ty::Mat: return "mat" + std::to_string(t.n) + "x" + std::to_string(t.r) + "<f32>";
+    case Ty::Arr: return "array<" + wgsl_name(elemT(t)) + ", " + std::to_string(t.alen) + ">";
+    case Ty::Struct: return g_structs && t.sid >= 0 ? (*g_structs)[size_t(t.sid)].name : "struct";
   }
   return "?";
 }
@@ -91,6 +129,8 @@ std::string cpp_name(const Ty& t) {
     case Ty::Scalar: return sk_cpp(t.s);
     case Ty::Vec: return std::string("::wgsl::vec<") + sk_cpp(t.s) + "," + std::to_string(t.n) + ">";
     case Ty::Mat: return "::wgsl::mat<" + std::to_string(t.n) + "," + std::to_string(t.r) + ">";
+    case Ty::Arr: return "::wgsl::arr<" + cpp_name(elemT(t)) + "," + std::to_string(t.alen) + ">";
+    case Ty::Struct: return "s_" + (g_structs && t.sid >= 0 ? (*g_structs)[size_t(t.sid)].name : std::string("?"));
   }
   return "?";
 }
@@ -113,11 +153,15 @@ SK concrete_sk(SK s) {
   return s;
 }
 Ty concretize(Ty t) {
-  if (t.cat == Ty::Scalar || t.cat == Ty::Vec) t.s = concrete_sk(t.s);
+  if (t.cat == Ty::Scalar || t.cat == Ty::Vec || t.cat == Ty::Arr) t.s = concrete_sk(t.s);
   return t;
 }
 bool ty_convertible(const Ty& from, const Ty& to) {
   if (from.cat != to.cat) return false;
+  if (from.cat == Ty::Struct) return from.sid == to.sid;
+  if (from.cat == Ty::Arr)
+    return from.alen == to.alen && from.ecat == to.ecat && from.n == to.n && from.r == to.r &&
+           from.sid == to.sid && convertible(from.s, to.s);
   if (from.cat == Ty::Vec && from.n != to.n) return false;
   if (from.cat == Ty::Mat) return from.n == to.n && from.r == to.r;
   if (from.cat == Ty::Void) return true;
@@ -301,7 +345,7 @@ struct Stmt;
 using SP = std::unique_ptr<Stmt>;
 struct Stmt {
   enum Kind { Let, Var, Const, Assign, Compound, Incr, Decr, Phony, ExprS, If, For, While, Loop,
-              Break, Continue, Return, Block, BreakIf } kind = ExprS;
+              Break, Continue, Return, Block, BreakIf, Switch } kind = ExprS;
   int line = 0, col = 0;
   std::string name, op;
   bool has_ty = false;
@@ -309,6 +353,14 @@ struct Stmt {
   EP e, lhs;
   std::vector<SP> body, els, continuing;
   SP init, update;
+  // switch: one clause per `case ...` / `default` with its selectors
+  struct Clause {
+    std::vector<EP> sel;
+    bool def = false;
+    std::vector<SP> body;
+    int line = 0, col = 0;
+  };
+  std::vector<Clause> clauses;
 };
 
 struct Param {
@@ -344,9 +396,23 @@ class Parser {
   explicit Parser(std::vector<Tok> toks) : t_(std::move(toks)) {}
 
   void module(std::vector<std::unique_ptr<Func>>& fns, std::vector<std::unique_ptr<GConst>>& consts) {
+    // struct names first: module-scope declarations may be used before
+    // they appear
+    for (size_t i = 0; i + 1 < t_.size(); ++i) {
+      if (t_[i].t == TT::Ident && t_[i].s == "struct" && t_[i + 1].t == TT::Ident) {
+        if (struct_id(t_[i + 1].s) >= 0) fail(t_[i + 1].line, t_[i + 1].col, "redefinition of struct '" + t_[i + 1].s + "'");
+        StructDef d;
+        d.name = t_[i + 1].s;
+        d.line = t_[i + 1].line;
+        d.col = t_[i + 1].col;
+        g_structs->push_back(d);
+      }
+    }
     while (!at_end()) {
       skip_attributes();
-      if (is_kw("fn")) {
+      if (is_kw("struct")) {
+        struct_decl();
+      } else if (is_kw("fn")) {
         fns.push_back(function());
       } else if (is_kw("const") || is_kw("let") || is_kw("override")) {
         if (is_kw("override")) fail(cur().line, cur().col, "override declarations are not supported");
@@ -360,7 +426,7 @@ class Parser {
         g->e = expr();
         expect(";");
         consts.push_back(std::move(g));
-      } else if (is_kw("struct") || is_kw("var") || is_kw("alias") || is_kw("enable")) {
+      } else if (is_kw("var") || is_kw("alias") || is_kw("enable")) {
         fail(cur().line, cur().col, "'" + cur().s + "' declarations are not supported in field function modules");
       } else if (cur().t == TT::Punct && cur().s == ";") {
         next();
@@ -375,6 +441,18 @@ class Parser {
   size_t p_ = 0;
 
   const Tok& cur() const { return t_[p_]; }
+  // Closes a template list: '>' or the first '>' of '>>' / '>=' / '>>='
+  // (vec3<vec3<f32>> style nesting), as WGSL's template disambiguation does.
+  void close_template() {
+    Tok& t = t_[p_];
+    if (t.t == TT::Punct && t.s == ">") { p_++; return; }
+    if (t.t == TT::Punct && (t.s == ">>" || t.s == ">=" || t.s == ">>=")) {
+      t.s = t.s.substr(1);
+      t.col++;
+      return;
+    }
+    fail(t.line, t.col, "expected '>', found '" + t.s + "'");
+  }
   const Tok& peek(int k = 1) const { return t_[std::min(p_ + k, t_.size() - 1)]; }
   bool at_end() const { return cur().t == TT::End; }
   Tok next() { Tok t = t_[p_]; if (p_ + 1 < t_.size()) ++p_; return t; }
@@ -407,6 +485,32 @@ class Parser {
     }
   }
 
+  // struct Name { member: type, ... }  (attributes on members are ignored)
+  void struct_decl() {
+    next();  // struct
+    Tok nt = cur();
+    const std::string name = ident("struct name");
+    StructDef& d = (*g_structs)[size_t(struct_id(name))];
+    expect("{");
+    while (!is_p("}")) {
+      if (at_end()) fail(cur().line, cur().col, "expected '}' before end of input");
+      skip_attributes();
+      Tok mt = cur();
+      const std::string m = ident("member name");
+      for (auto& x : d.members)
+        if (x.first == m) fail(mt.line, mt.col, "duplicate member '" + m + "' in struct '" + name + "'");
+      expect(":");
+      Ty t = type();
+      if (t.cat == Ty::Struct && t.sid == struct_id(name))
+        fail(mt.line, mt.col, "struct '" + name + "' cannot contain itself");
+      d.members.push_back({m, t});
+      if (!accept(",")) break;
+    }
+    expect("}");
+    accept(";");
+    if (d.members.empty()) fail(nt.line, nt.col, "struct '" + name + "' must have at least one member");
+  }
+
   static bool type_generator(const std::string& s) {
     return s == "vec2" || s == "vec3" || s == "vec4" || (s.size() == 6 && s.compare(0, 3, "mat") == 0 && s[4] == 'x') || s == "array";
   }
@@ -422,11 +526,16 @@ class Parser {
     if (n == "f16" || n == "f64") fail(k.line, k.col, "type '" + n + "' is not supported");
     Ty t;
     if (alias_type(n, t)) return t;
+    if (struct_id(n) >= 0) {
+      t.cat = Ty::Struct;
+      t.sid = struct_id(n);
+      return t;
+    }
     if (n == "vec2" || n == "vec3" || n == "vec4") {
       expect("<");
       Ty e = type();
       if (e.cat != Ty::Scalar) fail(k.line, k.col, "vector element must be a scalar type");
-      expect(">");
+      close_template();
       return vecT(e.s, n[3] - '0');
     }
     if (n.size() == 6 && n.compare(0, 3, "mat") == 0 && n[4] == 'x') {
@@ -435,10 +544,26 @@ class Parser {
       expect("<");
       Ty e = type();
       if (!(e.cat == Ty::Scalar && e.s == SK::F32)) fail(k.line, k.col, "matrix element type must be f32");
-      expect(">");
+      close_template();
       return matT(c, r);
     }
-    if (n == "array") fail(k.line, k.col, "array types are not supported in field functions");
+    if (n == "array") {
+      // array<E, N>: E a scalar, vector or matrix type, N an integer literal
+      expect("<");
+      Ty e = type();
+      if (e.cat == Ty::Arr) fail(k.line, k.col, "arrays of arrays are not supported in field functions");
+      if (e.cat == Ty::Void) fail(k.line, k.col, "invalid array element type");
+      if (is_p(">") || is_p(">>") || is_p(">="))
+        fail(cur().line, cur().col, "runtime-sized arrays are not allowed in a function; give the element count");
+      expect(",");
+      Tok nt = cur();
+      if (nt.t != TT::Int) fail(nt.line, nt.col, "array element count must be an integer literal");
+      next();
+      if (nt.iv <= 0 || nt.iv > 65536) fail(nt.line, nt.col, "array element count must be between 1 and 65536");
+      accept(",");
+      close_template();
+      return arrT(e, int(nt.iv));
+    }
     fail(k.line, k.col, "unknown type '" + n + "'");
   }
 
@@ -586,9 +711,48 @@ class Parser {
     if (is_kw("break")) { next(); expect(";"); return mk(Stmt::Break, at); }
     if (is_kw("continue")) { next(); expect(";"); return mk(Stmt::Continue, at); }
     if (is_kw("discard")) fail(at.line, at.col, "'discard' is only valid in fragment shaders");
-    if (is_kw("switch")) fail(at.line, at.col, "'switch' is not supported in field functions");
+    if (is_kw("switch")) return switch_stmt();
     SP s = simple_stmt();
     expect(";");
+    return s;
+  }
+
+  // switch_statement: 'switch' expression '{' clause+ '}'; a clause is
+  // 'case' selector (',' selector)* ','? ':'? compound, or 'default' ':'?
+  // compound; a selector is an expression or 'default'.
+  SP switch_stmt() {
+    Tok at = next();  // switch
+    SP s = mk(Stmt::Switch, at);
+    s->e = expr();
+    expect("{");
+    while (!is_p("}")) {
+      if (at_end()) fail(cur().line, cur().col, "expected '}' before end of input");
+      Stmt::Clause cl;
+      cl.line = cur().line;
+      cl.col = cur().col;
+      if (is_kw("default")) {
+        next();
+        cl.def = true;
+      } else if (is_kw("case")) {
+        next();
+        for (;;) {
+          if (is_kw("default")) {
+            next();
+            cl.def = true;
+          } else {
+            cl.sel.push_back(expr());
+          }
+          if (!accept(",")) break;
+          if (is_p(":") || is_p("{")) break;
+        }
+      } else {
+        fail(cur().line, cur().col, "expected 'case' or 'default' in switch");
+      }
+      accept(":");
+      cl.body = block();
+      s->clauses.push_back(std::move(cl));
+    }
+    expect("}");
     return s;
   }
 
@@ -795,7 +959,17 @@ class Parser {
       }
       std::string name = ident("expression");
       EP e;
-      if (type_generator(name) && is_p("<")) {
+      if (name == "bitcast" && is_p("<")) {
+        // bitcast<T>(e): reinterpret the bits of e as T
+        next();
+        Ty t = type();
+        close_template();
+        e = mkE(Expr::Call, at);
+        e->op = name;
+        e->has_targ = true;
+        e->targ = t;
+        if (!is_p("(")) fail(cur().line, cur().col, "expected '(' after bitcast<T>");
+      } else if (type_generator(name) && is_p("<")) {
         // templated constructor vec3<f32>(...) / mat3x3<f32>(...)
         p_--;  // re-read the generator as a type
         Ty t = type();
@@ -1025,6 +1199,8 @@ class Compiler {
     check(a);
     e.fl = a.fl;
     e.tr = a.tr;
+    if (a.ty.cat == Ty::Arr) fail(e.line, e.col, "operator '" + e.op + "' cannot be applied to an array");
+    if (a.ty.cat == Ty::Struct) fail(e.line, e.col, "operator '" + e.op + "' cannot be applied to a struct");
     if (e.op == "-") {
       if (!((a.ty.cat == Ty::Scalar || a.ty.cat == Ty::Vec) && is_numeric(a.ty.s)) && a.ty.cat != Ty::Mat)
         fail(e.line, e.col, "unary '-' needs a numeric operand, found " + wgsl_name(a.ty));
@@ -1057,6 +1233,10 @@ class Compiler {
     check(R);
     e.fl = L.fl + R.fl;
     e.tr = L.tr + R.tr;
+    if (L.ty.cat == Ty::Arr || R.ty.cat == Ty::Arr)
+      fail(e.line, e.col, "operator '" + e.op + "' cannot be applied to arrays");
+    if (L.ty.cat == Ty::Struct || R.ty.cat == Ty::Struct)
+      fail(e.line, e.col, "operator '" + e.op + "' cannot be applied to structs");
     const std::string& op = e.op;
     auto mismatch = [&]() -> void {
       fail(e.line, e.col, "no matching operator '" + op + "' for " + wgsl_name(L.ty) + " and " + wgsl_name(R.ty));
@@ -1201,6 +1381,17 @@ class Compiler {
     check(a);
     e.fl = a.fl;
     e.tr = a.tr;
+    if (a.ty.cat == Ty::Struct) {
+      for (auto& m : (*g_structs)[size_t(a.ty.sid)].members) {
+        if (m.first == e.op) {
+          e.ty = m.second;
+          e.lv = a.lv;
+          e.mut = a.mut;
+          return;
+        }
+      }
+      fail(e.line, e.col, "struct " + wgsl_name(a.ty) + " has no member '" + e.op + "'");
+    }
     if (a.ty.cat != Ty::Vec) fail(e.line, e.col, "type " + wgsl_name(a.ty) + " has no member '" + e.op + "'");
     const std::string& m = e.op;
     if (m.empty() || m.size() > 4) fail(e.line, e.col, "invalid swizzle '" + m + "'");
@@ -1234,6 +1425,11 @@ class Compiler {
     } else if (a.ty.cat == Ty::Mat) {
       if (i.cst && (i.cv < 0 || i.cv >= a.ty.n)) fail(i.line, i.col, "index out of bounds");
       e.ty = vecT(SK::F32, a.ty.r);
+    } else if (a.ty.cat == Ty::Arr) {
+      // a constant index is checked here; a runtime index is clamped to the
+      // array (wgpu's default bounds-check policy)
+      if (i.cst && (i.cv < 0 || i.cv >= a.ty.alen)) fail(i.line, i.col, "index out of bounds");
+      e.ty = elemT(a.ty);
     } else {
       fail(e.line, e.col, "cannot index a value of type " + wgsl_name(a.ty));
     }
@@ -1268,6 +1464,7 @@ class Compiler {
     if (n == "bool") { out = scalar(SK::Bool); return true; }
     if (Parser::alias_type(n, out)) return true;
     if (n == "vec2" || n == "vec3" || n == "vec4") { out = vecT(SK::AFloat, n[3] - '0'); inferred = true; return true; }
+    if (n == "array") { out = Ty(); out.cat = Ty::Arr; inferred = true; return true; }
     if (n.size() == 6 && n.compare(0, 3, "mat") == 0 && n[4] == 'x') {
       int c = n[3] - '0', r = n[5] - '0';
       if (c >= 2 && c <= 4 && r >= 2 && r <= 4) { out = matT(c, r); return true; }
@@ -1275,8 +1472,59 @@ class Compiler {
     return false;
   }
 
+  // bitcast<T>(e): T and e's type are i32 / u32 / f32 scalars, or vectors
+  // of them with the same component count.
+  void check_bitcast(Expr& e) {
+    if (!e.has_targ) fail(e.line, e.col, "bitcast needs a target type: bitcast<T>(e)");
+    need_args(e, 1);
+    const Ty t = e.targ;
+    const Ty a = concretize(e.args[0]->ty);
+    auto ok = [](const Ty& x) {
+      return (x.cat == Ty::Scalar || x.cat == Ty::Vec) && (x.s == SK::I32 || x.s == SK::U32 || x.s == SK::F32);
+    };
+    if (!ok(t)) fail(e.line, e.col, "bitcast target must be i32, u32, f32 or a vector of them, found " + wgsl_name(t));
+    if (!ok(a)) fail(e.line, e.col, "bitcast argument must be i32, u32, f32 or a vector of them, found " + wgsl_name(a));
+    if (t.cat != a.cat || (t.cat == Ty::Vec && t.n != a.n))
+      fail(e.line, e.col, "bitcast between types of different sizes: " + wgsl_name(a) + " to " + wgsl_name(t));
+    CallInfo ci;
+    ci.fn = "::wgsl::bitcast_<" + cpp_name(t) + ">";
+    ci.targets.push_back(a);
+    e.ty = t;
+    callinfo[&e] = ci;
+  }
+
+  // Name(m1, ..., mN): every member in declaration order; Name(): zero value.
+  void check_struct_ctor(Expr& e, int sid) {
+    const StructDef& d = (*g_structs)[size_t(sid)];
+    Ty t;
+    t.cat = Ty::Struct;
+    t.sid = sid;
+    e.ty = t;
+    CallInfo ci;
+    if (e.args.empty()) {
+      ci.kind = 5;
+      callinfo[&e] = ci;
+      return;
+    }
+    if (e.args.size() != d.members.size())
+      fail(e.line, e.col, "constructor of struct " + d.name + " needs " + std::to_string(d.members.size()) +
+                              " arguments, found " + std::to_string(e.args.size()));
+    for (size_t i = 0; i < e.args.size(); ++i) {
+      const Ty& mt = d.members[i].second;
+      const Ty& at = e.args[i]->ty;
+      if (!(at == mt || ty_convertible(at, mt)))
+        fail(e.args[i]->line, e.args[i]->col, "cannot convert " + wgsl_name(at) + " to " + wgsl_name(mt) +
+                                                  " (member '" + d.members[i].first + "')");
+      ci.targets.push_back(mt);
+    }
+    ci.kind = 1;
+    callinfo[&e] = ci;
+  }
+
   void check_call(Expr& e) {
     check_args(e);
+    if (e.op == "bitcast" && !fmap.count(e.op)) return check_bitcast(e);
+    if (!fmap.count(e.op) && struct_id(e.op) >= 0) return check_struct_ctor(e, struct_id(e.op));
     Ty ct;
     bool inferred;
     if (!fmap.count(e.op) && ctor_type(e, ct, inferred)) return check_ctor(e, ct, inferred);
@@ -1289,6 +1537,39 @@ class Compiler {
     CallInfo ci;
     ci.fn.clear();
     const size_t na = e.args.size();
+    if (t.cat == Ty::Arr) {
+      if (inferred) {
+        // array(e1, ..., eN): the element type is the common type of the
+        // arguments (abstract scalars made concrete)
+        if (na == 0) fail(e.line, e.col, "cannot infer the type of an empty array constructor");
+        Ty el = e.args[0]->ty;
+        for (auto& a : e.args) {
+          const Ty& at = a->ty;
+          if (at.cat != Ty::Scalar && at.cat != Ty::Vec && at.cat != Ty::Mat)
+            fail(a->line, a->col, "invalid array element " + wgsl_name(at));
+          if (at.cat != el.cat || at.n != el.n || at.r != el.r)
+            fail(a->line, a->col, "array elements of different types: " + wgsl_name(el) + " and " + wgsl_name(at));
+          SK u;
+          if (!unify_sk(el.s, at.s, u)) fail(a->line, a->col, "array elements of different types");
+          el.s = u;
+        }
+        t = arrT(concretize(el), int(na));
+      }
+      e.ty = t;
+      if (na == 0) { ci.kind = 5; callinfo[&e] = ci; return; }
+      if (int(na) != t.alen)
+        fail(e.line, e.col, wgsl_name(t) + " constructor needs " + std::to_string(t.alen) + " elements, found " +
+                                std::to_string(na));
+      const Ty el = elemT(t);
+      for (auto& a : e.args) {
+        if (!(a->ty == el || ty_convertible(a->ty, el)))
+          fail(a->line, a->col, "cannot convert " + wgsl_name(a->ty) + " to " + wgsl_name(el));
+        ci.targets.push_back(el);
+      }
+      ci.kind = 1;  // element-wise constructor
+      callinfo[&e] = ci;
+      return;
+    }
     if (t.cat == Ty::Scalar) {
       if (na == 0) { e.ty = t; ci.kind = 5; callinfo[&e] = ci; return; }
       if (na != 1 || e.args[0]->ty.cat != Ty::Scalar)
@@ -1496,6 +1777,10 @@ class Compiler {
 
   void check_builtin(Expr& e) {
     const std::string& n = e.op;
+    for (auto& a : e.args) {
+      if (a->ty.cat == Ty::Arr) fail(a->line, a->col, "built-in '" + n + "' does not take an array argument");
+      if (a->ty.cat == Ty::Struct) fail(a->line, a->col, "built-in '" + n + "' does not take a struct argument");
+    }
     CallInfo ci;
     ci.fn = "::wgsl::" + n;
     static const std::set<std::string> transc1 = {"sin", "cos", "tan", "asin", "acos", "atan", "sinh", "cosh",
@@ -1740,6 +2025,7 @@ class Compiler {
       }
       case Expr::Member: {
         std::string a = ex(*e.args[0]);
+        if (e.args[0]->ty.cat == Ty::Struct) return a + ".m_" + e.op;
         static const char* comp = "xyzw";
         if (e.op.size() == 1) return a + "." + comp[swz_index(e.op[0])];
         std::string s = "::wgsl::swz<";
@@ -1747,7 +2033,7 @@ class Compiler {
         return s + ">(" + a + ")";
       }
       case Expr::Index:
-        return ex(*e.args[0]) + "[" + ex_as(*e.args[1], scalar(SK::I32)) + "]";
+        return ex(*e.args[0]) + "[" + ex_as(*e.args[1], concretize(e.args[1]->ty)) + "]";
       case Expr::Call: {
         if (e.cst) return lit_as(e.cv, concretize(e.ty), e.line, e.col);
         CallInfo& ci = callinfo[&e];
@@ -1790,6 +2076,11 @@ class Compiler {
     if (s.kind == Stmt::Return) return true;
     if (s.kind == Stmt::Block) return returns(s.body);
     if (s.kind == Stmt::If) return !s.els.empty() && returns(s.body) && returns(s.els);
+    if (s.kind == Stmt::Switch) {
+      for (auto& cl : s.clauses)
+        if (!returns(cl.body)) return false;
+      return true;  // the checker requires a default clause
+    }
     if (s.kind == Stmt::Loop) {
       // a loop without break only leaves through return
       std::function<bool(const std::vector<SP>&)> has_break = [&](const std::vector<SP>& v) {
@@ -2022,13 +2313,71 @@ class Compiler {
         out += ind(d) + "}\n";
         return;
       }
+      case Stmt::Switch: {
+        check(*s.e);
+        const Ty st = s.e->ty;
+        if (!(st.cat == Ty::Scalar && is_int(st.s)))
+          fail(s.e->line, s.e->col, "'switch' selector must be i32 or u32, found " + wgsl_name(st));
+        c.fl += s.e->fl;
+        c.tr += s.e->tr;
+        SK want = st.s;
+        int n_default = 0;
+        for (auto& cl : s.clauses) {
+          if (cl.def) n_default++;
+          for (auto& e : cl.sel) {
+            check(*e);
+            if (!(e->ty.cat == Ty::Scalar && is_int(e->ty.s)))
+              fail(e->line, e->col, "case selector must be an integer, found " + wgsl_name(e->ty));
+            if (!e->cst && !(e->kind == Expr::Lit && e->lit == 1))
+              fail(e->line, e->col, "case selector must be a constant expression");
+            if (!is_abstract(e->ty.s)) {
+              if (is_abstract(want)) want = e->ty.s;
+              else if (e->ty.s != want)
+                fail(e->line, e->col, "case selector type " + wgsl_name(e->ty) + " does not match the selector's " +
+                                          std::string(sk_name(want)));
+            }
+          }
+        }
+        if (n_default != 1)
+          fail(s.line, s.col, n_default == 0 ? "switch statement must have a default clause"
+                                             : "switch statement has more than one default clause");
+        if (is_abstract(want)) want = SK::I32;
+        if (!is_abstract(st.s) && st.s != want)
+          fail(s.e->line, s.e->col, "switch selector type " + wgsl_name(st) + " does not match its case selectors");
+        std::set<long long> seen;
+        out += ind(d) + "switch (" + ex_as(*s.e, scalar(want)) + ") {\n";
+        Cost worst;
+        for (auto& cl : s.clauses) {
+          std::string labels;
+          for (auto& e : cl.sel) {
+            const long long v = e->cst ? (long long)e->cv : e->li;
+            const bool ok = want == SK::U32 ? (v >= 0 && v <= 0xffffffffLL) : (v >= INT32_MIN && v <= INT32_MAX);
+            if (!ok) fail(e->line, e->col, "case selector " + std::to_string(v) + " out of range for " + sk_name(want));
+            if (!seen.insert(v).second) fail(e->line, e->col, "duplicate case selector " + std::to_string(v));
+            labels += "case " + std::to_string(v) + (want == SK::U32 ? "u" : "") + ": ";
+          }
+          if (cl.def) labels += "default: ";
+          out += ind(d + 1) + labels + "{\n";
+          Cost cc;
+          switch_depth++;
+          stmts(cl.body, out, d + 2, cc);
+          switch_depth--;
+          out += ind(d + 1) + "} break;\n";
+          worst.fl = std::max(worst.fl, cc.fl);
+          worst.tr = std::max(worst.tr, cc.tr);
+        }
+        out += ind(d) + "}\n";
+        c.fl += worst.fl;
+        c.tr += worst.tr;
+        return;
+      }
       case Stmt::BreakIf:
         check(*s.e);
         if (!(s.e->ty.cat == Ty::Scalar && s.e->ty.s == SK::Bool)) fail(s.e->line, s.e->col, "'break if' condition must be bool");
         out += ind(d) + "if (" + ex(*s.e) + ") break;\n";
         return;
       case Stmt::Break:
-        if (loop_depth == 0) fail(s.line, s.col, "'break' outside of a loop");
+        if (loop_depth == 0 && switch_depth == 0) fail(s.line, s.col, "'break' outside of a loop or switch");
         out += ind(d) + "break;\n";
         return;
       case Stmt::Continue:
@@ -2042,6 +2391,7 @@ class Compiler {
   }
   std::vector<std::string> loop_labels;  // "" = C++ continue, else goto label
   int label_counter = 0;
+  int switch_depth = 0;  // break inside a switch clause leaves the switch
 
   static EP clone(const Expr& e) {
     EP c = std::make_unique<Expr>();
@@ -2067,11 +2417,13 @@ class Compiler {
     Func* saved_fn = cur_fn;
     auto saved_scopes = scopes;
     int saved_loop = loop_depth;
+    int saved_switch = switch_depth;
     auto saved_names = name_uses;
     name_uses.clear();
     scopes.clear();
     scopes.emplace_back();
     loop_depth = 0;
+    switch_depth = 0;
     cur_fn = &f;
     std::string params;
     for (size_t i = 0; i < f.params.size(); ++i) {
@@ -2094,6 +2446,7 @@ class Compiler {
     cur_fn = saved_fn;
     scopes = saved_scopes;
     loop_depth = saved_loop;
+    switch_depth = saved_switch;
     name_uses = saved_names;
     f.state = 2;
   }
@@ -2118,10 +2471,29 @@ Translation translate(const std::string& field_body, const std::string& helpers_
       "fn field_function(p_prev: vec3<f32>, p: vec3<f32>, v0: vec3<f32>, v: vec3<f32>, t: f32) -> vec3<f32> {\n";
   const std::string module = helpers_src + "\n" + header + field_body + "\n}\n";
   const int body_first_line = count_lines(helpers_src) + 3;  // 1-based line of the body
+  std::vector<StructDef> structs;
+  struct Reset {
+    ~Reset() { g_structs = nullptr; }
+  } reset;
+  g_structs = &structs;
   try {
     Parser ps(lex(module));
     Compiler cc;
     ps.module(cc.fns, cc.consts);
+    // structs may nest (by value) but not recursively; emit each after the
+    // structs its members contain
+    std::vector<int> state(structs.size(), 0), order;
+    std::function<void(int)> visit = [&](int i) {
+      if (state[size_t(i)] == 2) return;
+      const StructDef& d = structs[size_t(i)];
+      if (state[size_t(i)] == 1) throw CompileError(d.line, d.col, "struct '" + d.name + "' contains itself");
+      state[size_t(i)] = 1;
+      for (auto& m : d.members)
+        if ((m.second.cat == Ty::Struct || m.second.ecat == Ty::Struct) && m.second.sid >= 0) visit(m.second.sid);
+      state[size_t(i)] = 2;
+      order.push_back(i);
+    };
+    for (size_t i = 0; i < structs.size(); ++i) visit(int(i));
     cc.declare_module(0);
     Func* field = nullptr;
     for (auto& f : cc.fns)
@@ -2132,6 +2504,19 @@ Translation translate(const std::string& field_body, const std::string& helpers_
     std::ostringstream os;
     os << "// flops " << field->fl << " " << field->tr << " (FP32 arith, transcendental per evaluation)\n";
     os << "namespace " << ns << " {\n";
+    for (int i : order) {
+      const StructDef& d = structs[size_t(i)];
+      const std::string cn = "s_" + d.name;
+      os << "struct " << cn << " {\n";
+      for (auto& m : d.members) os << "  " << cpp_name(m.second) << " m_" << m.first << ";\n";
+      os << "  WG_HD " << cn << "() : ";
+      for (size_t k = 0; k < d.members.size(); ++k) os << (k ? ", " : "") << "m_" << d.members[k].first << "()";
+      os << " {}\n  WG_HD " << cn << "(";
+      for (size_t k = 0; k < d.members.size(); ++k) os << (k ? ", " : "") << cpp_name(d.members[k].second) << " a" << k;
+      os << ") : ";
+      for (size_t k = 0; k < d.members.size(); ++k) os << (k ? ", " : "") << "m_" << d.members[k].first << "(a" << k << ")";
+      os << " {}\n};\n";
+    }
     for (auto& c : cc.const_code) os << c << "\n";
     // prototypes (WGSL functions may be used before their declaration)
     for (auto& f : cc.fns) {
