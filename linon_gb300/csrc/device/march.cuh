@@ -561,10 +561,10 @@ __device__ __forceinline__ void march_plain_kernel(const F& field, const MarchAr
   const int W = a.frame.W, H = a.frame.H;
   const int lx = threadIdx.x % a.tile_w, ly = threadIdx.x / a.tile_w;
   const int x = blockIdx.x * a.tile_w + lx;
-  const int row = blockIdx.y * a.tile_h + ly;
+  const int row = a.row0 + blockIdx.y * a.tile_h + ly;
   // Threads outside the image stay in the warp as idle lanes (no early
   // exit) so that the per-step warp vote below always names all 32 lanes.
-  const bool in_image = x < W && row < H;
+  const bool in_image = x < W && row < a.row1;
   const int gy = H - 1 - row;
   const Basis b = make_basis(a.cam, W, H, a.m.focal_length, a.m.viewport_height);
   const vec3f dir = primary_dir(b, in_image ? x : 0, in_image ? gy : 0);

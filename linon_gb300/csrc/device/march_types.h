@@ -57,6 +57,7 @@ struct MarchArgs {
   DevScene scene;
   DevFrame frame;
   int tile_w, tile_h;
+  int row0, row1;          // rows [row0, row1) of the frame this launch covers
   int* err;                // device error word (bit 0: smem staging timeout)
 };
 

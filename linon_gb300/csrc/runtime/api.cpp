@@ -359,6 +359,13 @@ int linon_destroy(linon_ctx* ctx) {
   dev_free(ctx, ctx->host_io);
   linon::batch_release(ctx);
   if (ctx->d_err) cudaFree(ctx->d_err);
+  for (cudaStream_t s : ctx->band_stream)
+    if (s) cudaStreamDestroy(s);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+  for (cudaEvent_t e : ctx->band_done)
+    if (e) cudaEventDestroy(e);
+  if (ctx->band_start) cudaEventDestroy(ctx->band_start);
+  if (ctx->copies_done) cudaEventDestroy(ctx->copies_done);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return LINON_OK;
@@ -528,16 +535,23 @@ const char* linon_field_cuda_source(const linon_field* field) {
   return field ? field->cuda.c_str() : nullptr;
 }
 
-int linon_render(linon_ctx* ctx, const linon_field* field, const linon_camera* camera,
-                 const linon_settings* settings, const linon_march_params* params,
-                 const linon_frame* out) {
-  LINON_TRY_BEGIN
-  if (int st = enter(ctx)) return st;
+namespace {
+
+int render_checks(linon_ctx* ctx, const linon_field* field, const linon_camera* camera,
+                  const linon_march_params* params, int32_t width, int32_t height) {
   if (int st = field_valid(ctx, field)) return st;
-  if (!camera || !out) return set_error(LINON_EINVAL, "null camera or frame");
+  if (!camera) return set_error(LINON_EINVAL, "null camera");
   if (int st = check_params(params)) return st;
-  if (int st = check_frame_size(out->width, out->height)) return st;
-  if (!ctx->has_scene) return set_error(LINON_ENOSCENE, "linon_render before linon_scene_upload");
+  if (int st = check_frame_size(width, height)) return st;
+  if (!ctx->has_scene) return set_error(LINON_ENOSCENE, "render before linon_scene_upload");
+  return LINON_OK;
+}
+
+// One launch of the plain march kernel over rows [row0, row1) of the frame
+// (row0 a multiple of the 16-row tile).
+int launch_rows(linon_ctx* ctx, const linon_field* field, const linon_camera* camera,
+                const linon_settings* settings, const linon_march_params* params, const linon_frame* out,
+                int row0, int row1, cudaStream_t stream) {
   MarchArgs a;
   a.m = dev_march(settings, params);
   a.cam = dev_camera(camera);
@@ -550,15 +564,29 @@ int linon_render(linon_ctx* ctx, const linon_field* field, const linon_camera* c
   a.frame.steps = out->steps;
   a.tile_w = 8;
   a.tile_h = 16;
+  a.row0 = row0;
+  a.row1 = row1;
   a.err = ctx->d_err;
   cudaKernel_t k;
   const bool precise = (field->flags & LINON_COMPILE_PRECISE) != 0;
   if (int st = march_kernel(field, march_variant(params, settings, precise), &k)) return st;
-  dim3 grid((out->width + a.tile_w - 1) / a.tile_w, (out->height + a.tile_h - 1) / a.tile_h);
+  dim3 grid((out->width + a.tile_w - 1) / a.tile_w, (row1 - row0 + a.tile_h - 1) / a.tile_h);
   void* args[] = {&a};
   LINON_CUDA(cudaLaunchKernel((const void*)k, grid, dim3(a.tile_w * a.tile_h), args,
-                              size_t(a.scene.staged_bytes), ctx->stream));
+                              size_t(a.scene.staged_bytes), stream));
   return LINON_OK;
+}
+
+}  // namespace
+
+int linon_render(linon_ctx* ctx, const linon_field* field, const linon_camera* camera,
+                 const linon_settings* settings, const linon_march_params* params,
+                 const linon_frame* out) {
+  LINON_TRY_BEGIN
+  if (int st = enter(ctx)) return st;
+  if (!out) return set_error(LINON_EINVAL, "null frame");
+  if (int st = render_checks(ctx, field, camera, params, out->width, out->height)) return st;
+  return launch_rows(ctx, field, camera, settings, params, out, 0, out->height, ctx->stream);
   LINON_TRY_END
 }
 
@@ -583,7 +611,7 @@ int linon_render_host(linon_ctx* ctx, const linon_field* field, const linon_came
                       int32_t* steps) {
   LINON_TRY_BEGIN
   if (int st = enter(ctx)) return st;
-  if (int st = check_frame_size(width, height)) return st;
+  if (int st = render_checks(ctx, field, camera, params, width, height)) return st;
   const size_t n = size_t(width) * height;
   const size_t need = n * (4 + 16 + 4 + 4) + 64;
   if (int st = dev_alloc(ctx, ctx->host_io, need)) return st;
@@ -595,11 +623,45 @@ int linon_render_host(linon_ctx* ctx, const linon_field* field, const linon_came
   f.color = color ? reinterpret_cast<uint8_t*>(base + n * 16) : nullptr;
   f.hit_id = hit_id ? reinterpret_cast<int32_t*>(base + n * 20) : nullptr;
   f.steps = steps ? reinterpret_cast<int32_t*>(base + n * 24) : nullptr;
-  if (int st = linon_render(ctx, field, camera, settings, params, &f)) return st;
-  if (mapping) LINON_CUDA(cudaMemcpyAsync(mapping, f.mapping, n * 16, cudaMemcpyDeviceToHost, ctx->stream));
-  if (color) LINON_CUDA(cudaMemcpyAsync(color, f.color, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
-  if (hit_id) LINON_CUDA(cudaMemcpyAsync(hit_id, f.hit_id, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
-  if (steps) LINON_CUDA(cudaMemcpyAsync(steps, f.steps, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  // Bands of rows: each band's planes go to the host while later bands
+  // render (the kernel is compute-bound, the copies ride on the copy
+  // engine); consecutive bands alternate between two streams so one band's
+  // last CTAs overlap the next band's first.  Small frames take one band.
+  const int tile_h = 16;
+  const int nb = n >= (size_t(1) << 18) ? 8 : 1;
+  const int band = ((height + nb - 1) / nb + tile_h - 1) / tile_h * tile_h;
+  if (!ctx->copy_stream) {
+    for (auto& s : ctx->band_stream) LINON_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    LINON_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    for (auto& e : ctx->band_done) LINON_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    LINON_CUDA(cudaEventCreateWithFlags(&ctx->band_start, cudaEventDisableTiming));
+    LINON_CUDA(cudaEventCreateWithFlags(&ctx->copies_done, cudaEventDisableTiming));
+  }
+  // the bands start after the work already queued on the context's stream
+  LINON_CUDA(cudaEventRecord(ctx->band_start, ctx->stream));
+  for (auto s : ctx->band_stream) LINON_CUDA(cudaStreamWaitEvent(s, ctx->band_start, 0));
+  int b = 0;
+  for (int r0 = 0; r0 < height; r0 += band, ++b) {
+    const int r1 = std::min(height, r0 + band);
+    cudaStream_t s = ctx->band_stream[b & 1];
+    if (int st = launch_rows(ctx, field, camera, settings, params, &f, r0, r1, s)) return st;
+    LINON_CUDA(cudaEventRecord(ctx->band_done[b], s));
+    LINON_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->band_done[b], 0));
+    const size_t p0 = size_t(r0) * width, pn = size_t(r1 - r0) * width;
+    if (mapping)
+      LINON_CUDA(cudaMemcpyAsync(mapping + 4 * p0, f.mapping + 4 * p0, pn * 16, cudaMemcpyDeviceToHost,
+                                 ctx->copy_stream));
+    if (color)
+      LINON_CUDA(cudaMemcpyAsync(color + 4 * p0, f.color + 4 * p0, pn * 4, cudaMemcpyDeviceToHost,
+                                 ctx->copy_stream));
+    if (hit_id)
+      LINON_CUDA(cudaMemcpyAsync(hit_id + p0, f.hit_id + p0, pn * 4, cudaMemcpyDeviceToHost, ctx->copy_stream));
+    if (steps)
+      LINON_CUDA(cudaMemcpyAsync(steps + p0, f.steps + p0, pn * 4, cudaMemcpyDeviceToHost, ctx->copy_stream));
+  }
+  // later work on the context's stream follows the copies
+  LINON_CUDA(cudaEventRecord(ctx->copies_done, ctx->copy_stream));
+  LINON_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->copies_done, 0));
   return linon_synchronize(ctx);
   LINON_TRY_END
 }

@@ -122,6 +122,11 @@ struct linon_ctx {
   int* d_err = nullptr;
   linon::DevBuf scratch;       // grown on demand (capture positions, queues, ...)
   linon::DevBuf host_io;       // device planes for linon_render_host
+  // linon_render_host's band pipeline: two render streams (consecutive bands
+  // overlap at their tails) and one copy stream, created on first use
+  cudaStream_t band_stream[2] = {nullptr, nullptr};
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t band_start = nullptr, band_done[8] = {}, copies_done = nullptr;
   // batch tuning cache
   linon_batch_tuning tuned{};
   bool has_tuned = false;
