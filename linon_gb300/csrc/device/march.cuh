@@ -101,6 +101,14 @@ __device__ __forceinline__ bool box_overlap(const float4& lo, const float4& hi, 
 #define LINON_BVH_STACK 48
 #endif
 
+// Launch bounds of the batched kernels (up to 256-thread CTAs); defining
+// LINON_BATCH_MIN_CTAS adds the minimum resident CTAs per SM.
+#ifdef LINON_BATCH_MIN_CTAS
+#define LINON_BATCH_BOUNDS __launch_bounds__(256, LINON_BATCH_MIN_CTAS)
+#else
+#define LINON_BATCH_BOUNDS __launch_bounds__(256)
+#endif
+
 // Launch bounds of the plain march kernels (128-thread CTAs).  Defining
 // LINON_MARCH_MIN_CTAS adds the minimum resident CTAs per SM, which caps the
 // registers per thread (and may spill).
@@ -660,7 +668,12 @@ __device__ __forceinline__ int find_view(const BatchArgs& a, long long gid) {
   return lo;
 }
 
-template <class Fields>
+// MODE: 0 any views (the step variant is chosen per ray at run time);
+// 1 every view has a fixed step budget without Kahan sums; 2 the same with
+// Kahan sums.  The specialised modes carry no adaptive-step or unused-sum
+// state, which keeps the kernel's register count (and so its occupancy)
+// close to the plain kernel's.
+template <int MODE = 0, class Fields>
 __device__ __forceinline__ void march_batch_kernel(const Fields& fields, const BatchArgs& a) {
   extern __shared__ float4 linon_smem[];
   __shared__ unsigned long long mbar;
@@ -669,7 +682,7 @@ __device__ __forceinline__ void march_batch_kernel(const Fields& fields, const B
   const int lane = threadIdx.x & 31;
   RayState r;
   DevMarch m;
-  DevFrame out;
+  int vi = 0;  // view of the lane's ray (its output planes are read at the store)
   size_t pix = 0;
   int fidx = 0;
   bool active = false;
@@ -696,7 +709,7 @@ __device__ __forceinline__ void march_batch_kernel(const Fields& fields, const B
             const int row = (tile / V.tiles_x) * a.tile_h + within / a.tile_w;
             if (x < V.frame.W && row < V.frame.H) {
               m = V.m;
-              out = V.frame;
+              vi = view;
               fidx = V.field;
               pix = size_t(row) * V.frame.W + x;
               const Basis b = make_basis(V.cam, V.frame.W, V.frame.H, m.focal_length, m.viewport_height);
@@ -707,6 +720,7 @@ __device__ __forceinline__ void march_batch_kernel(const Fields& fields, const B
                 HitRec hit = intersect_segment(sc, b.origin, dir, 100.0f, b.origin + 100.0f * dir, a.err);
                 wgsl::vec4f c(0.0f, 0.0f, 0.0f, 0.0f);
                 if (hit.t > 0.0f && hit.t < 100.0f) c = shade_hit(sc, hit, dir);
+                const DevFrame& out = V.frame;
                 if (out.color) {
                   uchar4 o;
                   o.x = unorm8(c.x); o.y = unorm8(c.y); o.z = unorm8(c.z); o.w = unorm8(c.w);
@@ -734,10 +748,13 @@ __device__ __forceinline__ void march_batch_kernel(const Fields& fields, const B
       const bool go = active && ray_active(r, m);
       const unsigned g = __ballot_sync(FULL, go);
       if (g == 0u || (!drained && __popc(g) < a.refill_below)) break;
-      if (go) ray_step_rt(r, field, m, sc, a.err);
+      if (go) {
+        if (MODE == 0) ray_step_rt(r, field, m, sc, a.err);
+        else ray_step<false, MODE == 2>(r, field, m, sc, a.err);
+      }
     }
     if (active && !ray_active(r, m)) {
-      ray_store(r, out, pix);
+      ray_store(r, a.views[vi].frame, pix);
       active = false;
     }
   }

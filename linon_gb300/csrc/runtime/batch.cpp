@@ -50,8 +50,12 @@ std::string batch_module_source(const std::vector<const linon_field*>& fields) {
     s << "      case " << i << ": return linon_user_" << i << "::field_function(pp, p, v0, v, t);\n";
   s << "      default: return linon_user_0::field_function(pp, p, v0, v, t);\n"
        "    }\n  }\n};\n"
-       "extern \"C\" __global__ void __launch_bounds__(256) linon_batch(linon::BatchArgs a) {\n"
-       "  linon::march_batch_kernel(LinonFields(), a);\n}\n";
+       "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_batch(linon::BatchArgs a) {\n"
+       "  linon::march_batch_kernel<0>(LinonFields(), a);\n}\n"
+       "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_batch_f(linon::BatchArgs a) {\n"
+       "  linon::march_batch_kernel<1>(LinonFields(), a);\n}\n"
+       "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_batch_fk(linon::BatchArgs a) {\n"
+       "  linon::march_batch_kernel<2>(LinonFields(), a);\n}\n";
   return s.str();
 }
 
@@ -84,7 +88,7 @@ int get_module(linon_ctx* ctx, BatchState& bs, const linon_field* const* fields,
   }
   std::string log;
   const bool precise = (fv[0]->flags & LINON_COMPILE_PRECISE) != 0;
-  int st = jit_compile(batch_module_source(fv), precise, {"linon_batch"}, mod, log);
+  int st = jit_compile(batch_module_source(fv), precise, {"linon_batch", "linon_batch_f", "linon_batch_fk"}, mod, log);
   if (st != LINON_OK) return set_error(st, st == LINON_ECOMPILE ? log : std::string(linon_last_error()));
   bs.modules[key] = mod;
   (void)ctx;
@@ -210,9 +214,19 @@ int batch_module(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fie
   return get_module(ctx, g_batch[ctx], fields, n_fields, mod);
 }
 
+const char* batch_kernel_name(const linon_view* views, int n_views) {
+  bool kahan = false, plain = false;
+  for (int i = 0; i < n_views; ++i) {
+    if (views[i].params.adaptive) return "linon_batch";
+    (views[i].params.kahan ? kahan : plain) = true;
+  }
+  if (kahan && plain) return "linon_batch";
+  return kahan ? "linon_batch_fk" : "linon_batch_f";
+}
+
 int batch_launch(linon_ctx* ctx, const std::shared_ptr<JitModule>& mod, const linon_batch_tuning& t,
                  const BatchView* views_dev, int n_views, long long total_rays,
-                 unsigned long long* counter, cudaStream_t stream) {
+                 unsigned long long* counter, cudaStream_t stream, const char* kernel) {
   BatchArgs a;
   std::memset(&a, 0, sizeof a);
   a.views = views_dev;
@@ -225,7 +239,7 @@ int batch_launch(linon_ctx* ctx, const std::shared_ptr<JitModule>& mod, const li
   a.tile_h = t.tile_h;
   a.refill_below = t.refill_below;
   a.err = ctx->d_err;
-  cudaKernel_t k = mod->kernels.at("linon_batch");
+  cudaKernel_t k = mod->kernels.at(kernel);
   int sms = 0;
   LINON_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   int per_sm = t.ctas_per_sm;
@@ -289,7 +303,7 @@ int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields, int32_t
     a.tile_h = t.tile_h;
     a.refill_below = t.refill_below;
     a.err = ctx->d_err;
-    cudaKernel_t k = mod->kernels.at("linon_batch");
+    cudaKernel_t k = mod->kernels.at(batch_kernel_name(views, n_views));
     int sms = 0;
     LINON_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
     int per_sm = t.ctas_per_sm;

@@ -87,9 +87,13 @@ long long batch_table(const linon_view* views, int n_views, const linon_batch_tu
                       std::vector<BatchView>& tab);
 int batch_module(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fields,
                  std::shared_ptr<JitModule>& mod);
+// The batched kernel for a set of views: linon_batch_f / linon_batch_fk when
+// no view refines its step adaptively and all (or none) use Kahan sums,
+// otherwise the generic linon_batch.
+const char* batch_kernel_name(const linon_view* views, int n_views);
 int batch_launch(linon_ctx* ctx, const std::shared_ptr<JitModule>& mod, const linon_batch_tuning& t,
                  const BatchView* views_dev, int n_views, long long total_rays,
-                 unsigned long long* counter, cudaStream_t stream);
+                 unsigned long long* counter, cudaStream_t stream, const char* kernel);
 
 }  // namespace linon
 

@@ -215,7 +215,8 @@ int launch_wave(linon_server* s, Slot& sl) {
     const long long total = batch_table(views.data(), int(views.size()), s->tuning, tab);
     LINON_CUDA(cudaMemcpyAsync(sl.views_dev, tab.data(), sizeof(BatchView) * tab.size(), cudaMemcpyHostToDevice,
                                sl.main));
-    if (int st = batch_launch(ctx, s->mod, s->tuning, sl.views_dev, int(views.size()), total, sl.counter, sl.main))
+    if (int st = batch_launch(ctx, s->mod, s->tuning, sl.views_dev, int(views.size()), total, sl.counter, sl.main,
+                              batch_kernel_name(views.data(), int(views.size()))))
       return st;
     for (size_t i = 0; i < renders.size(); ++i) {
       Request* q = renders[i];
