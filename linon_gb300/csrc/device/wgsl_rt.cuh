@@ -173,6 +173,13 @@ template <class A> WG_HD A div_pow_k(const A& a, float x, float k) {
 // ---------------------------------------------------------------------------
 template <class T, int N> struct vec;
 
+// (s * v) / pow(x, k) and (v * s) / pow(x, k), s a scalar, v a vector:
+// precise modules evaluate as written; fast modules form the scalar factor
+// s * pow(x, -k) first and scale v once (one multiply per component instead
+// of two).
+template <class V> WG_HD V div_pow_k_sv(float s, const V& v, float x, float k);
+template <class V> WG_HD V div_pow_k_vs(const V& v, float s, float x, float k);
+
 template <class T> struct vec<T, 2> {
   T x, y;
   WG_HD vec() : x(T(0)), y(T(0)) {}
@@ -226,6 +233,21 @@ struct arr {
   WG_HD T& operator[](unsigned i) { return v[i >= unsigned(N) ? unsigned(N - 1) : i]; }
   WG_HD const T& operator[](unsigned i) const { return v[i >= unsigned(N) ? unsigned(N - 1) : i]; }
 };
+
+template <class V> WG_HD V div_pow_k_sv(float s, const V& v, float x, float k) {
+#if !defined(LINON_PRECISE) && defined(__CUDA_ARCH__)
+  return v * (s * pow_k(x, -k));
+#else
+  return (s * v) / powf(x, k);
+#endif
+}
+template <class V> WG_HD V div_pow_k_vs(const V& v, float s, float x, float k) {
+#if !defined(LINON_PRECISE) && defined(__CUDA_ARCH__)
+  return v * (s * pow_k(x, -k));
+#else
+  return (v * s) / powf(x, k);
+#endif
+}
 
 // bitcast<T>(e): the bits of a 32-bit scalar (or of each vector component)
 // reinterpreted as another 32-bit scalar type.

@@ -183,10 +183,23 @@ int batch_tuning(const linon_ctx* ctx, const linon_batch_tuning* in, linon_batch
 long long batch_table(const linon_view* views, int n_views, const linon_batch_tuning& t,
                       std::vector<BatchView>& tab) {
   tab.assign(static_cast<size_t>(n_views), BatchView());
-  long long begin = 0;
+  // Queue order: views with the largest step budget per ray first, so that
+  // when the queue drains the SMs finish on short rays (longest-first list
+  // scheduling); each table entry carries its own outputs, so the order is
+  // free.  Budget: max_steps, or t_max / h for the t-loop.
+  std::vector<int> order(static_cast<size_t>(n_views));
+  std::vector<double> budget(static_cast<size_t>(n_views));
   for (int i = 0; i < n_views; ++i) {
+    const linon_march_params& p = views[i].params;
+    order[size_t(i)] = i;
+    budget[size_t(i)] = p.max_steps > 0 ? double(p.max_steps) : double(p.t_max) / double(p.h_initial);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return budget[size_t(a)] > budget[size_t(b)]; });
+  long long begin = 0;
+  for (int k = 0; k < n_views; ++k) {
+    const int i = order[size_t(k)];
     const linon_view& v = views[i];
-    BatchView& b = tab[size_t(i)];
+    BatchView& b = tab[size_t(k)];
     b.m = to_dev(v.settings, v.params);
     for (int k = 0; k < 3; ++k) {
       b.cam.o[k] = v.camera.origin[k];

@@ -2006,9 +2006,25 @@ class Compiler {
         if (op == "/" && is_float(e.ty.s)) {
           Expr& R = *e.args[1];
           auto ci = callinfo.find(&R);
-          if (R.kind == Expr::Call && !R.cst && ci != callinfo.end() && ci->second.fn == "::wgsl::pow_k")
-            return "::wgsl::div_pow_k(" + a + ", " + ex_as(*R.args[0], ci->second.targets[0]) + ", " +
-                   ex_as(*R.args[1], ci->second.targets[1]) + ")";
+          if (R.kind == Expr::Call && !R.cst && ci != callinfo.end() && ci->second.fn == "::wgsl::pow_k") {
+            const std::string xk = ex_as(*R.args[0], ci->second.targets[0]) + ", " +
+                                   ex_as(*R.args[1], ci->second.targets[1]);
+            // (s * V) / pow(x, k) with a scalar s and a vector V: fast
+            // modules scale V once by s * pow(x, -k) (div_pow_k_sv)
+            Expr& L = *e.args[0];
+            if (L.kind == Expr::Binary && L.op == "*" && !L.cst && e.ty.cat == Ty::Vec) {
+              BinInfo& li = bininfo[&L];
+              const bool s0 = L.args[0]->ty.cat == Ty::Scalar && L.args[1]->ty.cat == Ty::Vec;
+              const bool s1 = L.args[1]->ty.cat == Ty::Scalar && L.args[0]->ty.cat == Ty::Vec;
+              if (s0)
+                return "::wgsl::div_pow_k_sv(" + ex_as(*L.args[0], li.tl) + ", " + ex_as(*L.args[1], li.tr) + ", " +
+                       xk + ")";
+              if (s1)
+                return "::wgsl::div_pow_k_vs(" + ex_as(*L.args[0], li.tl) + ", " + ex_as(*L.args[1], li.tr) + ", " +
+                       xk + ")";
+            }
+            return "::wgsl::div_pow_k(" + a + ", " + xk + ")";
+          }
         }
         if (vec) {
           if (op == "<") return "::wgsl::cmp_lt(" + a + ", " + b + ")";

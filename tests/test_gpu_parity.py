@@ -157,6 +157,41 @@ def test_fast_vs_fp64_1080p(engine, oracle, name):
         assert err.max() <= 1e-4, err.max()
 
 
+def test_plain_small_512_config(engine, oracle):
+    """The 512x512 twist workload (h = 0.01, 1000 steps, per-face colours):
+    the precise module against the FP32 oracle and the fast module within
+    1e-4 of the FP64 oracle, on 2000 seeded pixels of the full frame (hit
+    mismatch <= 0.1% outside coplanar ties)."""
+    w = wl.plain_small()
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    rng = np.random.default_rng(5)
+    pix = np.sort(rng.choice(w.width * w.height, 2000, replace=False)).astype(np.int32)
+    fid = _abi.FIELD_IDS["twist"]
+    gp = gpu_render(engine, w, field(engine, "twist", True))
+    o32 = oracle.render(w.xyz, w.faces, w.face_rgb, w.camera, w.settings, w.params, fid, w.width, w.height,
+                        pixels=pix, want=("color", "mapping", "hit_id", "steps"))
+    # sin/cos are CUDA's in the module and the C library's in the oracle
+    # (last-bit differences): hit ids on >= 99.5% of the pixels, endpoints of
+    # the agreeing pixels within 1e-5
+    same = gp["hit_id"].ravel()[pix] == o32["hit_id"]
+    assert same.mean() >= 0.995, same.mean()
+    np.testing.assert_array_equal(gp["steps"].ravel()[pix], o32["steps"])
+    d32 = np.abs(gp["mapping"].reshape(-1, 4)[pix, :3] - o32["mapping"][:, :3]).max(-1)
+    assert np.percentile(d32[same], 99) <= 1e-5, np.percentile(d32[same], 99)
+    gf = gpu_render(engine, w, field(engine, "twist", False))
+    o64 = oracle.render(w.xyz, w.faces, w.face_rgb, w.camera, w.settings, w.params, fid, w.width, w.height,
+                        pixels=pix, precision=64, want=("mapping64", "hit_id", "steps"))
+    err = np.abs(gf["mapping"].reshape(-1, 4)[pix, :3].astype(np.float64) - o64["mapping64"][:, :3]).max(-1)
+    gh = gf["hit_id"].ravel()[pix]
+    groups = scene.coplanar_groups(w.xyz, w.faces)
+    diff = gh != o64["hit_id"]
+    tie = diff & (gh >= 0) & (o64["hit_id"] >= 0)
+    tie[tie] = groups[gh[tie]] == groups[o64["hit_id"][tie]]
+    assert np.mean(diff & ~tie) <= 0.001
+    assert err.max() <= 1e-4, err.max()
+    assert (gf["steps"] == 1000).all()
+
+
 def test_fast_math_accuracy(engine):
     """Fast modules' sin/cos (one Cody-Waite reduction by 2 pi, then the
     special-function unit on r = x - k 2 pi) and constant-exponent pow
@@ -225,6 +260,31 @@ def test_odd_and_tiny_sizes(engine, oracle, size):
     np.testing.assert_array_equal(np.isnan(g["mapping"]), np.isnan(o["mapping"]))
     m = ~np.isnan(o["mapping"])
     np.testing.assert_array_equal(g["mapping"][m], o["mapping"][m])
+
+
+def test_frame_size_limits(engine, oracle):
+    """The largest accepted width (65535) renders like the oracle; sizes
+    beyond the limits (65536 per side, 2^31 - 1 pixels, zero) are rejected
+    with LINON_EINVAL before any output pointer is touched."""
+    import ctypes as C
+    w = steps_case()
+    w.params = wl.fixed_steps(0.05, 8)
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    fld = field(engine, "linear", True)
+    g = gpu_render(engine, w, fld, 65535, 2)
+    cols = np.r_[0:64, 32000:32064, 65471:65535]
+    pix = np.concatenate([cols, 65535 + cols]).astype(np.int32)
+    o = oracle.render(w.xyz, w.faces, w.face_rgb, w.camera, w.settings, w.params, _abi.FIELD_IDS["linear"], 65535, 2,
+                      pixels=pix, want=("mapping", "hit_id", "steps"))
+    np.testing.assert_array_equal(g["hit_id"].ravel()[pix], o["hit_id"])
+    np.testing.assert_array_equal(g["mapping"].reshape(-1, 4)[pix].view(np.uint32), o["mapping"].view(np.uint32))
+    lib = _abi.load()
+    for W, H in ((65536, 1), (1, 65536), (65535, 65535), (0, 5), (5, -1)):
+        f = _abi.Frame()
+        f.width, f.height = W, H  # null planes: only the size check may run
+        st = lib.linon_render(engine.ctx, fld.handle, C.byref(w.camera), C.byref(w.settings), C.byref(w.params),
+                              C.byref(f))
+        assert st == _abi.LINON_EINVAL, (W, H, st)
 
 
 def test_empty_scene_and_linear_mode(engine, oracle):
