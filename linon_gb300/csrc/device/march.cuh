@@ -120,6 +120,13 @@ __device__ __forceinline__ bool box_overlap(const float4& lo, const float4& hi, 
 
 
 // Segment query; seg_end is origin + step (the unnormalised step vector).
+// PAIR selects the walk: false visits one node per iteration (the smallest
+// code, best for the small scenes staged in shared memory); true tests both
+// children of an inner node when it is reached, descends only into the
+// overlapping ones and loads each node record once (fewer iterations and
+// loads on deep trees read through L1).  Both test the triangles of the
+// leaves whose boxes and all ancestors' boxes overlap the segment's box.
+template <bool PAIR = false>
 __device__ __forceinline__ HitRec intersect_segment(const SceneView& sc, const vec3f& origin,
                                                     const vec3f& direction, float max_dist,
                                                     const vec3f& seg_end, int* err) {
@@ -134,30 +141,64 @@ __device__ __forceinline__ HitRec intersect_segment(const SceneView& sc, const v
   vec3f smin = wgsl::min(origin, seg_end), smax = wgsl::max(origin, seg_end);
   int stack[LINON_BVH_STACK];
   int sp = 0;
-  int node = 0;
-  for (;;) {
-    const float4 lo = sc.nodes[2 * node];
-    const float4 hi = sc.nodes[2 * node + 1];
-    bool visit = box_overlap(lo, hi, smin, smax);
-    if (visit) {
-      int first = __float_as_int(lo.w);
-      int count = __float_as_int(hi.w);
-      if (count > 0) {
-        for (int i = 0; i < count; ++i) test_tri(sc, first + i, origin, direction, max_dist, best);
-      } else {
-        if (sp < LINON_BVH_STACK) {
-          stack[sp++] = first + 1;
+  if (!PAIR) {
+    int node = 0;
+    for (;;) {
+      const float4 lo = sc.nodes[2 * node];
+      const float4 hi = sc.nodes[2 * node + 1];
+      if (box_overlap(lo, hi, smin, smax)) {
+        const int first = __float_as_int(lo.w);
+        const int count = __float_as_int(hi.w);
+        if (count > 0) {
+          for (int i = 0; i < count; ++i) test_tri(sc, first + i, origin, direction, max_dist, best);
         } else {
-          // The host caps the tree depth below the stack size, so this is
-          // unreachable; if it ever were reached the flag reports it.
-          atomicOr(err, 2);
+          if (sp < LINON_BVH_STACK) {
+            stack[sp++] = first + 1;
+          } else {
+            // The host caps the tree depth below the stack size, so this is
+            // unreachable; if it ever were reached the flag reports it.
+            atomicOr(err, 2);
+          }
+          node = first;
+          continue;
         }
-        node = first;
+      }
+      if (sp == 0) break;
+      node = stack[--sp];
+    }
+    return best;
+  }
+  float4 lo = sc.nodes[0], hi = sc.nodes[1];
+  if (!box_overlap(lo, hi, smin, smax)) return best;
+  for (;;) {
+    const int first = __float_as_int(lo.w);
+    const int count = __float_as_int(hi.w);
+    if (count > 0) {
+      for (int i = 0; i < count; ++i) test_tri(sc, first + i, origin, direction, max_dist, best);
+    } else {
+      const float4 lo0 = sc.nodes[2 * first], hi0 = sc.nodes[2 * first + 1];
+      const float4 lo1 = sc.nodes[2 * first + 2], hi1 = sc.nodes[2 * first + 3];
+      const bool o0 = box_overlap(lo0, hi0, smin, smax);
+      const bool o1 = box_overlap(lo1, hi1, smin, smax);
+      if (o0) {
+        if (o1) {
+          if (sp < LINON_BVH_STACK) stack[sp++] = first + 1;
+          else atomicOr(err, 2);  // unreachable: the host caps the depth
+        }
+        lo = lo0;
+        hi = hi0;
+        continue;
+      }
+      if (o1) {
+        lo = lo1;
+        hi = hi1;
         continue;
       }
     }
     if (sp == 0) break;
-    node = stack[--sp];
+    const int node = stack[--sp];
+    lo = sc.nodes[2 * node];
+    hi = sc.nodes[2 * node + 1];
   }
   return best;
 }
@@ -372,7 +413,9 @@ enum { V_ADAPTIVE = 1, V_KAHAN = 2, V_STEPS = 4, V_W1 = 8 };
 
 // One attempted RK4 step (main_view.wgsl:245-270).  Returns false when the
 // step was rejected by the adaptive rule (h refined, nothing advanced).
-template <bool ADAPTIVE, bool KAHAN, bool W1 = false, class F>
+// PAIR: the BVH walk of intersect_segment (child-pair for the batched
+// kernels, which read large scenes through L1).
+template <bool ADAPTIVE, bool KAHAN, bool W1 = false, bool PAIR = false, class F>
 __device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevMarch& m,
                                          const SceneView& sc, int* err) {
   const float h = r.h;
@@ -412,7 +455,7 @@ __device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevM
 #else
       const vec3f dirn = wgsl::normalize(step_dir);
 #endif
-      HitRec hit = intersect_segment(sc, r.p, dirn, len, seg_end, err);
+      HitRec hit = intersect_segment<PAIR>(sc, r.p, dirn, len, seg_end, err);
       if (hit.t > 0.0f && hit.t < len) {
         r.color = shade_hit(sc, hit, dirn);
         r.has_color = r.color.w > 0.0f;
@@ -640,11 +683,11 @@ template <class F>
 __device__ __forceinline__ void ray_step_rt(RayState& r, const F& field, const DevMarch& m,
                                             const SceneView& sc, int* err) {
   if (m.adaptive) {
-    if (m.kahan) ray_step<true, true>(r, field, m, sc, err);
-    else ray_step<true, false>(r, field, m, sc, err);
+    if (m.kahan) ray_step<true, true, false, true>(r, field, m, sc, err);
+    else ray_step<true, false, false, true>(r, field, m, sc, err);
   } else {
-    if (m.kahan) ray_step<false, true>(r, field, m, sc, err);
-    else ray_step<false, false>(r, field, m, sc, err);
+    if (m.kahan) ray_step<false, true, false, true>(r, field, m, sc, err);
+    else ray_step<false, false, false, true>(r, field, m, sc, err);
   }
 }
 
@@ -750,7 +793,7 @@ __device__ __forceinline__ void march_batch_kernel(const Fields& fields, const B
       if (g == 0u || (!drained && __popc(g) < a.refill_below)) break;
       if (go) {
         if (MODE == 0) ray_step_rt(r, field, m, sc, a.err);
-        else ray_step<false, MODE == 2>(r, field, m, sc, a.err);
+        else ray_step<false, MODE == 2, false, true>(r, field, m, sc, a.err);
       }
     }
     if (active && !ray_active(r, m)) {
