@@ -2095,7 +2095,7 @@ class Compiler {
     if (s.kind == Stmt::Switch) {
       for (auto& cl : s.clauses)
         if (!returns(cl.body)) return false;
-      return true;  // the checker requires a default clause
+      return true;  // the type check requires a default clause
     }
     if (s.kind == Stmt::Loop) {
       // a loop without break only leaves through return

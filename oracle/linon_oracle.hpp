@@ -1,8 +1,9 @@
 // linon_oracle.hpp — CPU restatement of linon's ray-casting path.
 //
-// TEST INFRASTRUCTURE ONLY.  This header is the checker for the CUDA engine
-// in linon_gb300/: only tests/, __graft_entry__.smoke() and bench.py's CPU
-// baseline leg may use it, and never as the thing measured or shipped.
+// TEST INFRASTRUCTURE ONLY.  This header is the oracle the CUDA engine in
+// linon_gb300/ is compared against: only tests/, __graft_entry__.smoke() and
+// bench.py's CPU baseline leg may use it, and never as the thing measured or
+// shipped.
 //
 // It restates, operation for operation and in the shader's evaluation order,
 //   src/main_view.wgsl:78-146  helpers (rotateX/Y/Z, translate, refraction_index,

@@ -1,8 +1,8 @@
 """ctypes wrapper of the oracle library (oracle/_build/liblinon_oracle.so).
 
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py as the checker of the CUDA engine; never as the
-thing measured or shipped.  The oracle is the C++ restatement of the shader
+CPU-baseline leg of bench.py as the oracle the CUDA engine is compared
+against; never as the thing measured or shipped.  The oracle is the C++ restatement of the shader
 path in oracle/linon_oracle.hpp (parity against the reference itself is
 unpinned: the reference is WGSL run through a graphics API, which is not
 available here).

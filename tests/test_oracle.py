@@ -89,7 +89,7 @@ def test_t_loop_step_counts(oracle):
         r = oracle.render(xyz, faces, None, cam.arcball_default(center), wl.settings(), p,
                           _abi.FIELD_IDS["linear"], 8, 8, pixels=[0])
         assert r["steps"][0] == n
-    # the survey's worked example: 500 steps at h = 0.01 (exact arithmetic: 501)
+    # worked example: 500 steps at h = 0.01 in f32 (exact arithmetic: 501)
     t, n = np.float32(0.0), 0
     while t <= np.float32(5.0):
         t = np.float32(t + np.float32(0.01))
