@@ -28,10 +28,11 @@ using wgsl::vec3f;
 #endif
 
 // --------------------------------------------------------------------------
-// Scene access.  Triangles are three float4 each: (v0, face id bits),
-// (e1 = v1 - v0, 0), (e2 = v2 - v0, 0); e1/e2 are the differences
-// hit_triangle computes (IEEE subtraction, so precomputing them changes
-// nothing).  BVH nodes are two float4: (lo.xyz, first), (hi.xyz, count);
+// Scene access.  Triangles are four float4 each: (v0, face id bits),
+// (e1 = v1 - v0, 0), (e2 = v2 - v0, 0), (unit normal n, d = n . v0); e1/e2
+// are the differences hit_triangle computes (IEEE subtraction, so
+// precomputing them changes nothing); the plane (zero for a degenerate
+// triangle) only serves conservative culling.  BVH nodes are two float4: (lo.xyz, first), (hi.xyz, count);
 // count > 0 is a leaf over triangles [first, first+count), otherwise the
 // children are nodes first and first+1.  Node boxes are inflated on the host
 // so that culling never drops a triangle the brute-force loop would hit.
@@ -43,6 +44,9 @@ struct SceneView {
   int n_tris;
   int n_nodes;
   float margin;
+  const float* grid;  // distance grid (see DevScene), NULL: none
+  int gx, gy, gz;
+  float gox, goy, goz, gcell, ginv;
 };
 
 __device__ __forceinline__ vec3f xyz(const float4& a) { return vec3f(a.x, a.y, a.z); }
@@ -77,9 +81,18 @@ struct HitRec {
 // lower face index (the brute-force loop's strict `<`, main_view.wgsl:193).
 __device__ __forceinline__ void test_tri(const SceneView& sc, int slot, const vec3f& origin,
                                          const vec3f& direction, float max_dist, HitRec& best) {
-  const float4 A = sc.tris[3 * slot];
-  const float4 B = sc.tris[3 * slot + 1];
-  const float4 C = sc.tris[3 * slot + 2];
+  // A segment whose two ends lie on the same side of the triangle's plane,
+  // both farther than the culling margin, cannot produce a hit inside the
+  // segment (the rounding of the plane distances and of hit_triangle is
+  // orders of magnitude below the margin): skip the full test.
+  const float4 P = sc.tris[4 * slot + 3];
+  const vec3f n = xyz(P);
+  const float s0 = wgsl::dot(origin, n) - P.w;
+  const float s1 = fmaf(max_dist, wgsl::dot(direction, n), s0);
+  if ((s0 > sc.margin && s1 > sc.margin) || (s0 < -sc.margin && s1 < -sc.margin)) return;
+  const float4 A = sc.tris[4 * slot];
+  const float4 B = sc.tris[4 * slot + 1];
+  const float4 C = sc.tris[4 * slot + 2];
   float t_new = hit_triangle(xyz(A), xyz(B), xyz(C), origin, direction);
   if (t_new > 0.0f && t_new < max_dist) {
     int id = __float_as_int(A.w);
@@ -222,11 +235,9 @@ __device__ __forceinline__ float leaf_bound2(const SceneView& sc, int first, int
                                              const vec3f& q, float margin) {
   float pmin = 3.0e38f;
   for (int i = 0; i < count; ++i) {
-    const float4 A = sc.tris[3 * (first + i)];
-    const vec3f n = wgsl::cross(xyz(sc.tris[3 * (first + i) + 1]), xyz(sc.tris[3 * (first + i) + 2]));
-    const vec3f d = q - xyz(A);
-    // a degenerate triangle gives NaN here, which fmaxf turns into 0
-    const float pd = fabsf(wgsl::dot(d, n)) * rsqrtf(wgsl::dot(n, n)) - margin;
+    // a degenerate triangle has a zero plane: distance 0, bound 0
+    const float4 P = sc.tris[4 * (first + i) + 3];
+    const float pd = fabsf(wgsl::dot(q, xyz(P)) - P.w) - margin;
     pmin = fminf(pmin, fmaxf(pd, 0.0f));
   }
   return fmaxf(box_d2, pmin * pmin);
@@ -271,11 +282,40 @@ __device__ __forceinline__ float nearest_leaf_bound(const SceneView& sc, const v
   return best >= 3.0e38f ? 3.0e38f : sqrtf(best) * 0.99999f;
 }
 
+// Centre of grid cell (ix, iy, iz); the grid build and the queries use this
+// same expression.
+__device__ __forceinline__ vec3f grid_centre(const SceneView& sc, int ix, int iy, int iz) {
+  return vec3f(fmaf(float(ix) + 0.5f, sc.gcell, sc.gox), fmaf(float(iy) + 0.5f, sc.gcell, sc.goy),
+               fmaf(float(iz) + 0.5f, sc.gcell, sc.goz));
+}
+
+// Radius of a safe ball around q: every point closer to q than the result is
+// outside every margin-inflated leaf box (hence farther than the culling
+// margin from every triangle).  With a distance grid: the bound stored at
+// the centre c of q's cell minus |q - c| (triangle inequality); outside the
+// grid: the distance to the root box, which holds every leaf box.  Without
+// a grid: the BVH query.  The result is shrunk by a relative 1e-5 and 1e-6
+// absolute against the rounding of the differences.
+__device__ __forceinline__ float safe_radius(const SceneView& sc, const vec3f& q) {
+  if (sc.grid) {
+    const float fx = (q.x - sc.gox) * sc.ginv, fy = (q.y - sc.goy) * sc.ginv, fz = (q.z - sc.goz) * sc.ginv;
+    if (fx >= 0.0f && fy >= 0.0f && fz >= 0.0f && fx < float(sc.gx) && fy < float(sc.gy) && fz < float(sc.gz)) {
+      const int ix = int(fx), iy = int(fy), iz = int(fz);
+      const float c = sc.grid[(size_t(iz) * sc.gy + iy) * sc.gx + ix];
+      const float b = c - wgsl::length(q - grid_centre(sc, ix, iy, iz));
+      return fmaxf(b * 0.99999f - 1e-6f, 0.0f);
+    }
+    if (!(q.x == q.x && q.y == q.y && q.z == q.z)) return 0.0f;
+    return fmaxf(sqrtf(box_dist2(sc.nodes[0], sc.nodes[1], q)) * 0.99999f - 1e-6f, 0.0f);
+  }
+  return nearest_leaf_bound(sc, q, sc.margin);
+}
+
 // Shading of ray_color, main_view.wgsl:199-217 (camera is the light source).
 __device__ __forceinline__ wgsl::vec4f shade_hit(const SceneView& sc, const HitRec& hit,
                                                  const vec3f& direction) {
-  const vec3f d1 = xyz(sc.tris[3 * hit.slot + 1]);
-  const vec3f d2 = xyz(sc.tris[3 * hit.slot + 2]);
+  const vec3f d1 = xyz(sc.tris[4 * hit.slot + 1]);
+  const vec3f d2 = xyz(sc.tris[4 * hit.slot + 2]);
   vec3f normal = wgsl::normalize(wgsl::cross(d1, d2));
   float intensity = wgsl::max(wgsl::dot(normal, -direction), 0.0f);
   if (intensity == 0.0f) intensity = wgsl::max(wgsl::dot(-normal, -direction), 0.0f);
@@ -467,7 +507,7 @@ __device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevM
           r.cool--;
         } else {
           // a new ball around the segment's end, where the next one starts
-          const float b = nearest_leaf_bound(sc, seg_end, sc.margin);
+          const float b = safe_radius(sc, seg_end);
           r.q0 = seg_end;
           r.safe2 = b * b;
           // close to geometry the ball buys little: test plainly for a while
@@ -580,6 +620,15 @@ __device__ __forceinline__ SceneView cta_scene(const DevScene& s, float4* smem,
   v.n_tris = s.n_tris;
   v.n_nodes = s.n_nodes;
   v.margin = s.margin;
+  v.grid = s.grid;
+  v.gx = s.gx;
+  v.gy = s.gy;
+  v.gz = s.gz;
+  v.gox = s.gox;
+  v.goy = s.goy;
+  v.goz = s.goz;
+  v.gcell = s.gcell;
+  v.ginv = s.ginv;
   if (s.staged_bytes > 0) {
     // staged block = [nodes | tris] contiguous in global memory
     if (stage_to_smem(smem, s.staged, (unsigned)s.staged_bytes, mbar, err)) {

@@ -33,7 +33,7 @@ struct DevCamera {
 };
 
 struct DevScene {
-  const float4* tris;      // 3 float4 per triangle (see march.cuh)
+  const float4* tris;      // 4 float4 per triangle (see march.cuh)
   const float4* nodes;     // 2 float4 per BVH node, NULL = brute force
   const float4* face_rgb;  // optional per-face colour (by original face index)
   const float4* staged;    // contiguous [nodes | tris] block for smem staging
@@ -41,6 +41,12 @@ struct DevScene {
   int n_nodes;
   int staged_bytes;        // 0 = read the scene from global memory
   float margin;            // inflation of the BVH boxes (culling margin)
+  // distance grid (NULL: none): at each cell centre a lower bound on the
+  // distance to every margin-inflated BVH leaf box
+  const float* grid;
+  int gx, gy, gz;          // cells per axis
+  float gox, goy, goz;     // corner of cell (0, 0, 0)
+  float gcell, ginv;       // cell size and its inverse
 };
 
 struct DevFrame {

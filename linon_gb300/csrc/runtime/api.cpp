@@ -95,19 +95,6 @@ DevCamera dev_camera(const linon_camera* c) {
   return d;
 }
 
-DevScene dev_scene(const linon_ctx* ctx) {
-  DevScene s;
-  const float4* block = static_cast<const float4*>(ctx->scene_block.p);
-  s.nodes = ctx->n_nodes ? block : nullptr;
-  s.tris = block + 2 * size_t(ctx->n_nodes);
-  s.face_rgb = static_cast<const float4*>(ctx->face_rgb.p);
-  s.staged = block;
-  s.n_tris = ctx->n_tris;
-  s.n_nodes = ctx->n_nodes;
-  s.staged_bytes = ctx->staged_bytes;
-  s.margin = ctx->margin;
-  return s;
-}
 
 int check_frame_size(int32_t W, int32_t H) {
   if (W <= 0 || H <= 0) return set_error(LINON_EINVAL, "image size must be positive");
@@ -279,6 +266,31 @@ int launch_capture(linon_ctx* ctx, const linon_field* field, const linon_camera*
 
 using namespace linon;
 
+namespace linon {
+DevScene dev_scene(const linon_ctx* ctx) {
+  DevScene s;
+  const float4* block = static_cast<const float4*>(ctx->scene_block.p);
+  s.nodes = ctx->n_nodes ? block : nullptr;
+  s.tris = block + 2 * size_t(ctx->n_nodes);
+  s.face_rgb = static_cast<const float4*>(ctx->face_rgb.p);
+  s.staged = block;
+  s.n_tris = ctx->n_tris;
+  s.n_nodes = ctx->n_nodes;
+  s.staged_bytes = ctx->staged_bytes;
+  s.margin = ctx->margin;
+  s.grid = static_cast<const float*>(ctx->grid.p);
+  s.gx = ctx->gx;
+  s.gy = ctx->gy;
+  s.gz = ctx->gz;
+  s.gox = ctx->gox;
+  s.goy = ctx->goy;
+  s.goz = ctx->goz;
+  s.gcell = ctx->gcell;
+  s.ginv = ctx->gcell > 0.0f ? 1.0f / ctx->gcell : 0.0f;
+  return s;
+}
+}  // namespace linon
+
 extern "C" {
 
 int linon_abi_version(void) { return LINON_ABI_VERSION; }
@@ -357,6 +369,7 @@ int linon_destroy(linon_ctx* ctx) {
   dev_free(ctx, ctx->face_rgb);
   dev_free(ctx, ctx->scratch);
   dev_free(ctx, ctx->host_io);
+  dev_free(ctx, ctx->grid);
   linon::batch_release(ctx);
   if (ctx->d_err) cudaFree(ctx->d_err);
   for (cudaStream_t s : ctx->band_stream)
@@ -408,6 +421,7 @@ int linon_scene_upload(linon_ctx* ctx, const float* xyz, uint32_t n_vertices, co
   LINON_CUDA(cudaStreamSynchronize(ctx->stream));
   dev_free(ctx, ctx->scene_block);
   dev_free(ctx, ctx->face_rgb);
+  dev_free(ctx, ctx->grid);
   ctx->has_scene = false;
   if (int st = dev_alloc(ctx, ctx->scene_block, std::max<size_t>(bytes, 16))) return st;
   if (!b.nodes.empty())
@@ -429,6 +443,45 @@ int linon_scene_upload(linon_ctx* ctx, const float* xyz, uint32_t n_vertices, co
   ctx->margin = b.margin;
   // small scenes are staged in shared memory by one TMA bulk copy per CTA
   ctx->staged_bytes = bytes <= 16384 && bytes > 0 ? int(bytes) : 0;
+  // distance grid over the root box plus a border of two cells, 128 cells
+  // along the longest axis (at most 2^22 cells); skipped when the HBM budget
+  // cannot hold it (the march then queries the BVH)
+  dev_free(ctx, ctx->grid);
+  ctx->gx = ctx->gy = ctx->gz = 0;
+  ctx->gcell = 0.0f;
+  if (!b.nodes.empty()) {
+    const float4 lo = b.nodes[0], hi = b.nodes[1];
+    const float ext[3] = {hi.x - lo.x, hi.y - lo.y, hi.z - lo.z};
+    const float emax = std::max(ext[0], std::max(ext[1], ext[2]));
+    if (std::isfinite(emax) && emax > 0.0f) {
+      float cell = emax / 128.0f;
+      int dims[3];
+      for (;;) {
+        size_t total = 1;
+        for (int k = 0; k < 3; ++k) {
+          dims[k] = int(std::ceil(ext[k] / cell)) + 4;
+          total *= size_t(dims[k]);
+        }
+        if (total <= (size_t(1) << 22)) break;
+        cell *= 1.25f;
+      }
+      const size_t gbytes = sizeof(float) * size_t(dims[0]) * dims[1] * dims[2];
+      if (!ctx->budget || ctx->device_bytes + gbytes <= ctx->budget) {
+        if (int st = dev_alloc(ctx, ctx->grid, gbytes)) return st;
+        ctx->gx = dims[0];
+        ctx->gy = dims[1];
+        ctx->gz = dims[2];
+        ctx->gox = lo.x - 2.0f * cell;
+        ctx->goy = lo.y - 2.0f * cell;
+        ctx->goz = lo.z - 2.0f * cell;
+        ctx->gcell = cell;
+        ctx->has_scene = true;
+        const DevScene s = dev_scene(ctx);
+        LINON_CUDA(launch_grid_build(s, static_cast<float*>(ctx->grid.p), ctx->stream));
+        LINON_CUDA(cudaStreamSynchronize(ctx->stream));
+      }
+    }
+  }
   ctx->has_scene = true;
   return LINON_OK;
   LINON_TRY_END

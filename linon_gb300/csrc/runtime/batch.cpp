@@ -112,20 +112,6 @@ DevMarch to_dev(const linon_settings& st, const linon_march_params& mp) {
   return m;
 }
 
-DevScene scene_of(const linon_ctx* ctx) {
-  DevScene s;
-  const float4* block = static_cast<const float4*>(ctx->scene_block.p);
-  s.nodes = ctx->n_nodes ? block : nullptr;
-  s.tris = block + 2 * size_t(ctx->n_nodes);
-  s.face_rgb = static_cast<const float4*>(ctx->face_rgb.p);
-  s.staged = block;
-  s.n_tris = ctx->n_tris;
-  s.n_nodes = ctx->n_nodes;
-  s.staged_bytes = ctx->staged_bytes;
-  s.margin = ctx->margin;
-  return s;
-}
-
 int validate_batch(const linon_ctx* ctx, const linon_field* const* fields, int32_t n_fields,
                    const linon_view* views, int32_t n_views) {
   if (!ctx) return set_error(LINON_EINVAL, "null context");
@@ -247,7 +233,7 @@ int batch_launch(linon_ctx* ctx, const std::shared_ptr<JitModule>& mod, const li
   a.quantum = t.quantum;
   a.total_rays = total_rays;
   a.counter = counter;
-  a.scene = scene_of(ctx);
+  a.scene = dev_scene(ctx);
   a.tile_w = t.tile_w;
   a.tile_h = t.tile_h;
   a.refill_below = t.refill_below;
@@ -311,7 +297,7 @@ int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields, int32_t
     a.quantum = t.quantum;
     a.total_rays = begin;
     a.counter = static_cast<unsigned long long*>(bs.counter.p);
-    a.scene = scene_of(ctx);
+    a.scene = dev_scene(ctx);
     a.tile_w = t.tile_w;
     a.tile_h = t.tile_h;
     a.refill_below = t.refill_below;

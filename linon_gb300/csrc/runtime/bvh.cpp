@@ -136,9 +136,43 @@ void push_tri(std::vector<float4>& tris, const float* xyz, const uint32_t* abc, 
   const float* b = xyz + 3 * size_t(abc[3 * f + 1]);
   const float* c = xyz + 3 * size_t(abc[3 * f + 2]);
   // edge1 = v1 - v0, edge2 = v2 - v0 exactly as hit_triangle computes them
+  const float e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+  const float e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
   tris.push_back(make_float4(a[0], a[1], a[2], int_bits(int(f))));
-  tris.push_back(make_float4(b[0] - a[0], b[1] - a[1], b[2] - a[2], 0.0f));
-  tris.push_back(make_float4(c[0] - a[0], c[1] - a[1], c[2] - a[2], 0.0f));
+  tris.push_back(make_float4(e1[0], e1[1], e1[2], 0.0f));
+  tris.push_back(make_float4(e2[0], e2[1], e2[2], 0.0f));
+  // unit plane for conservative culling (double, rounded once); zero for a
+  // degenerate or non-finite triangle
+  const double n[3] = {double(e1[1]) * e2[2] - double(e1[2]) * e2[1], double(e1[2]) * e2[0] - double(e1[0]) * e2[2],
+                       double(e1[0]) * e2[1] - double(e1[1]) * e2[0]};
+  const double len = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  if (len > 0.0 && std::isfinite(len)) {
+    const float nx = float(n[0] / len), ny = float(n[1] / len), nz = float(n[2] / len);
+    const double d = double(nx) * a[0] + double(ny) * a[1] + double(nz) * a[2];
+    tris.push_back(make_float4(nx, ny, nz, float(d)));
+  } else {
+    tris.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+  }
+}
+
+// Culling margin: 2e-4 of the scene extent plus a few ulps of the largest
+// coordinate (far above the FP32 rounding of the plane distances and of the
+// Moeller-Trumbore quantities for points near the scene).
+float scene_margin(const float* xyz, const uint32_t* abc, uint32_t nf) {
+  float smin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, smax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  float amax = 0.0f;
+  for (uint32_t f = 0; f < nf; ++f)
+    for (int j = 0; j < 3; ++j) {
+      const float* v = xyz + 3 * size_t(abc[3 * f + j]);
+      for (int k = 0; k < 3; ++k) {
+        smin[k] = std::min(smin[k], v[k]);
+        smax[k] = std::max(smax[k], v[k]);
+        amax = std::max(amax, std::fabs(v[k]));
+      }
+    }
+  if (nf == 0) return 1e-7f;
+  const float extent = std::max(smax[0] - smin[0], std::max(smax[1] - smin[1], smax[2] - smin[2]));
+  return 2e-4f * extent + 8.0f * FLT_EPSILON * amax + 1e-7f;
 }
 
 }  // namespace
@@ -149,15 +183,14 @@ void build_scene_arrays(const float* xyz, uint32_t nv, const uint32_t* abc, uint
   out.nodes.clear();
   out.tris.clear();
   out.max_depth = 0;
-  out.tris.reserve(size_t(nf) * 3);
+  out.tris.reserve(size_t(nf) * 4);
+  out.margin = scene_margin(xyz, abc, nf);
   if (!bvh || nf == 0) {
     for (uint32_t f = 0; f < nf; ++f) push_tri(out.tris, xyz, abc, f);
     return;
   }
   Builder B;
   B.prims.resize(nf);
-  float smin[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, smax[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-  float amax = 0.0f;
   for (uint32_t f = 0; f < nf; ++f) {
     Prim& p = B.prims[f];
     for (int k = 0; k < 3; ++k) {
@@ -169,16 +202,11 @@ void build_scene_arrays(const float* xyz, uint32_t nv, const uint32_t* abc, uint
       for (int k = 0; k < 3; ++k) {
         p.lo[k] = std::min(p.lo[k], v[k]);
         p.hi[k] = std::max(p.hi[k], v[k]);
-        smin[k] = std::min(smin[k], v[k]);
-        smax[k] = std::max(smax[k], v[k]);
-        amax = std::max(amax, std::fabs(v[k]));
       }
     }
     for (int k = 0; k < 3; ++k) p.c[k] = 0.5f * (p.lo[k] + p.hi[k]);
   }
-  float extent = std::max(smax[0] - smin[0], std::max(smax[1] - smin[1], smax[2] - smin[2]));
-  // margin: 2e-4 of the scene extent plus a few ulps of the largest coordinate
-  B.margin = 2e-4f * extent + 8.0f * FLT_EPSILON * amax + 1e-7f;
+  B.margin = out.margin;
   B.idx.resize(nf);
   for (uint32_t i = 0; i < nf; ++i) B.idx[i] = i;
   B.nodes.resize(2);

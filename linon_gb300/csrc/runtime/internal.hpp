@@ -78,6 +78,9 @@ struct BvhBuild {
 void build_scene_arrays(const float* xyz, uint32_t nv, const uint32_t* abc, uint32_t nf,
                         bool bvh, BvhBuild& out);
 
+// Scene pointers and parameters of a context for the kernels (api.cpp).
+DevScene dev_scene(const linon_ctx* ctx);
+
 // Frees the batch tables, graphs and modules of a context (batch.cpp).
 void batch_release(linon_ctx* ctx);
 
@@ -122,6 +125,10 @@ struct linon_ctx {
   uint32_t max_depth = 0;
   float margin = 0.0f;
   int staged_bytes = 0;
+  // distance grid of the safe-ball radius (empty: the BVH query is used)
+  linon::DevBuf grid;
+  int gx = 0, gy = 0, gz = 0;
+  float gox = 0.0f, goy = 0.0f, goz = 0.0f, gcell = 0.0f;
   // device error word and scratch
   int* d_err = nullptr;
   linon::DevBuf scratch;       // grown on demand (capture positions, queues, ...)

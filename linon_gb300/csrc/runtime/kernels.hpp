@@ -29,6 +29,8 @@ struct FtleArgs {
 };
 
 cudaError_t launch_overlay(const OverlayArgs& a, bool fp64, cudaStream_t s);
+// Fills the distance grid of s (s.gx * s.gy * s.gz floats) from its BVH.
+cudaError_t launch_grid_build(const DevScene& s, float* grid, cudaStream_t stream);
 cudaError_t launch_ftle(const FtleArgs& a, cudaStream_t s);
 // slots: 9 u64 (8 selection keys + a found counter)
 cudaError_t launch_outline(const float* e, int W, int H, float min_exp, unsigned long long* slots,
