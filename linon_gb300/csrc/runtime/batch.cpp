@@ -150,7 +150,8 @@ int batch_tuning(const linon_ctx* ctx, const linon_batch_tuning* in, linon_batch
   t = linon_batch_tuning{};
   if (in) t = *in;
   else if (ctx->has_tuned) t = ctx->tuned;
-  if (t.quantum <= 0) t.quantum = 32;
+  // default: refill a warp when all its lanes are done (see the autotuner)
+  if (t.quantum <= 0) t.quantum = 1024;
   // 0: refill only at the end of a quantum (measured best on the 64-view
   // workload: an early refill costs a queue atomic and a camera set-up)
   if (t.refill_below < 0) t.refill_below = 0;
@@ -159,8 +160,8 @@ int batch_tuning(const linon_ctx* ctx, const linon_batch_tuning* in, linon_batch
   if (t.block_threads % 32 || t.block_threads > 256)
     return set_error(LINON_EINVAL, "block_threads must be a multiple of 32, <= 256");
   if (t.tile_w <= 0 || t.tile_h <= 0) {
-    t.tile_w = 8;
-    t.tile_h = 4;
+    t.tile_w = 4;
+    t.tile_h = 8;
   }
   if (t.tile_w * t.tile_h != 32) return set_error(LINON_EINVAL, "tile_w * tile_h must be 32");
   return LINON_OK;
@@ -359,10 +360,14 @@ int linon_autotune_batch(linon_ctx* ctx, const linon_field* const* fields, int32
                          const linon_view* views, int32_t n_views, linon_batch_tuning* best,
                          double* best_ms) {
   if (int st = validate_batch(ctx, fields, n_fields, views, n_views)) return st;
-  const int quanta[] = {16, 32, 64};
+  // Since the safe-ball radius comes from the distance grid, a warp that
+  // refills only when all its lanes are done (quantum >= the step budget)
+  // is fastest on the uneven-view workload (q 64: 23.3 ms, q 256: 21.4 ms,
+  // q 1024: 20.2 ms; early refill slower at every quantum).
+  const int quanta[] = {256, 1024, 4096};
   const int blocks[] = {128, 256};
   const int tiles[][2] = {{8, 4}, {4, 8}};
-  const int refills[] = {0, 16, 24};
+  const int refills[] = {0, 8};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);

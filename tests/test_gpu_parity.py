@@ -497,7 +497,12 @@ def test_batch_graph_replay_and_tuning(engine):
         for k in x:
             np.testing.assert_array_equal(x[k], y[k])
     t, ms = engine.autotune_batch(flds, views)
-    assert t.quantum in (8, 16, 32, 64) and ms > 0
+    assert t.quantum in (256, 1024, 4096) and t.refill_below in (0, 8) and ms > 0
+    # the tuned launch gives the same planes as the default one
+    engine.render_batch(flds, views, t)
+    for x, y in zip(first, snapshot(planes)):
+        for k in x:
+            np.testing.assert_array_equal(x[k], y[k])
 
 
 def test_hbm_budget_admission():
