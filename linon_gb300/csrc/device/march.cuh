@@ -45,6 +45,9 @@ struct SceneView {
   int n_nodes;
   float margin;
   const float* grid;  // distance grid (see DevScene), NULL: none
+  const int2* cells;  // per-cell candidate lists (see DevScene), NULL: none
+  const int* cell_tris;
+  float reach;
   int gx, gy, gz;
   float gox, goy, goz, gcell, ginv;
 };
@@ -289,6 +292,34 @@ __device__ __forceinline__ vec3f grid_centre(const SceneView& sc, int ix, int iy
                fmaf(float(iz) + 0.5f, sc.gcell, sc.goz));
 }
 
+// Segment test through the candidate list of the cell holding the segment's
+// start when the lists apply (a segment no longer than `reach` that starts in
+// a listed cell can only meet the listed triangles: every leaf box within
+// the cell's half diagonal plus `reach` of its centre is listed), otherwise
+// the BVH walk.  The same triangles' Moeller-Trumbore results decide, so the
+// hit is the BVH's (and the brute-force loop's).
+template <bool PAIR>
+__device__ __forceinline__ HitRec intersect_segment_cells(const SceneView& sc, const vec3f& origin,
+                                                          const vec3f& direction, float max_dist,
+                                                          const vec3f& seg_end, int* err) {
+  if (sc.cells && max_dist <= sc.reach) {
+    const float fx = (origin.x - sc.gox) * sc.ginv, fy = (origin.y - sc.goy) * sc.ginv,
+                fz = (origin.z - sc.goz) * sc.ginv;
+    if (fx >= 0.0f && fy >= 0.0f && fz >= 0.0f && fx < float(sc.gx) && fy < float(sc.gy) && fz < float(sc.gz)) {
+      const int2 l = sc.cells[(size_t(int(fz)) * sc.gy + int(fy)) * sc.gx + int(fx)];
+      if (l.y >= 0) {
+        HitRec best;
+        best.t = -1.0f;
+        best.id = 0x7fffffff;
+        best.slot = -1;
+        for (int k = 0; k < l.y; ++k) test_tri(sc, sc.cell_tris[l.x + k], origin, direction, max_dist, best);
+        return best;
+      }
+    }
+  }
+  return intersect_segment<PAIR>(sc, origin, direction, max_dist, seg_end, err);
+}
+
 // Radius of a safe ball around q: every point closer to q than the result is
 // outside every margin-inflated leaf box (hence farther than the culling
 // margin from every triangle).  With a distance grid: the bound stored at
@@ -495,7 +526,7 @@ __device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevM
 #else
       const vec3f dirn = wgsl::normalize(step_dir);
 #endif
-      HitRec hit = intersect_segment<PAIR>(sc, r.p, dirn, len, seg_end, err);
+      HitRec hit = intersect_segment_cells<PAIR>(sc, r.p, dirn, len, seg_end, err);
       if (hit.t > 0.0f && hit.t < len) {
         r.color = shade_hit(sc, hit, dirn);
         r.has_color = r.color.w > 0.0f;
@@ -621,6 +652,9 @@ __device__ __forceinline__ SceneView cta_scene(const DevScene& s, float4* smem,
   v.n_nodes = s.n_nodes;
   v.margin = s.margin;
   v.grid = s.grid;
+  v.cells = s.cells;
+  v.cell_tris = s.cell_tris;
+  v.reach = s.reach;
   v.gx = s.gx;
   v.gy = s.gy;
   v.gz = s.gz;

@@ -47,6 +47,12 @@ struct DevScene {
   int gx, gy, gz;          // cells per axis
   float gox, goy, goz;     // corner of cell (0, 0, 0)
   float gcell, ginv;       // cell size and its inverse
+  // per-cell candidate triangles (NULL: none): cells[i] = (start, count)
+  // into cell_tris (triangle slots), count -1 = use the BVH; valid for
+  // segments of length <= reach that start in the cell
+  const int2* cells;
+  const int* cell_tris;
+  float reach;
 };
 
 struct DevFrame {

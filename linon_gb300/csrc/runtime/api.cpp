@@ -61,6 +61,46 @@ void dev_free(linon_ctx* ctx, DevBuf& b) {
   b.bytes = 0;
 }
 
+// Candidate triangle lists of the distance grid's cells (segment test
+// without a BVH walk): a segment of length <= reach = 2 cells starting in a
+// cell can only meet triangles of the leaves within the cell's half
+// diagonal plus reach of its centre.  Cells with more than 64 candidates
+// keep the BVH.  Skipped (BVH only) when the HBM budget cannot hold them.
+int build_cell_lists(linon_ctx* ctx) {
+  const size_t n = size_t(ctx->gx) * ctx->gy * ctx->gz;
+  if (n == 0) return LINON_OK;
+  const float reach = 2.0f * ctx->gcell;
+  const float build_reach = (0.5f * std::sqrt(3.0f) * ctx->gcell + reach) * 1.0001f;
+  const int max_list = 64;
+  if (ctx->budget && ctx->device_bytes + n * (sizeof(int2) + sizeof(int)) > ctx->budget) return LINON_OK;
+  DevBuf counts;
+  if (int st = dev_alloc(ctx, counts, n * sizeof(int))) return st;
+  DevScene s = dev_scene(ctx);
+  cudaError_t e = launch_cell_count(s, build_reach, max_list, static_cast<int*>(counts.p), ctx->stream);
+  std::vector<int> hc(n);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hc.data(), counts.p, n * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  dev_free(ctx, counts);
+  if (e != cudaSuccess) return cuda_error(e, "cell list count");
+  std::vector<int2> lists(n);
+  long long total = 0;
+  for (size_t i = 0; i < n; ++i) {
+    lists[i] = make_int2(int(total), hc[i]);
+    if (hc[i] > 0) total += hc[i];
+  }
+  if (total >= (1ll << 31) - 1) return LINON_OK;
+  const size_t tbytes = sizeof(int) * size_t(std::max<long long>(total, 1));
+  if (ctx->budget && ctx->device_bytes + n * sizeof(int2) + tbytes > ctx->budget) return LINON_OK;
+  if (int st = dev_alloc(ctx, ctx->cells, n * sizeof(int2))) return st;
+  if (int st = dev_alloc(ctx, ctx->cell_tris, tbytes)) return st;
+  LINON_CUDA(cudaMemcpyAsync(ctx->cells.p, lists.data(), n * sizeof(int2), cudaMemcpyHostToDevice, ctx->stream));
+  LINON_CUDA(launch_cell_fill(s, build_reach, static_cast<const int2*>(ctx->cells.p),
+                              static_cast<int*>(ctx->cell_tris.p), ctx->stream));
+  LINON_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->reach = reach;
+  return LINON_OK;
+}
+
 int enter(linon_ctx* ctx) {
   if (!ctx) return set_error(LINON_EINVAL, "null context");
   cudaError_t e = cudaSetDevice(ctx->device);
@@ -287,6 +327,9 @@ DevScene dev_scene(const linon_ctx* ctx) {
   s.goz = ctx->goz;
   s.gcell = ctx->gcell;
   s.ginv = ctx->gcell > 0.0f ? 1.0f / ctx->gcell : 0.0f;
+  s.cells = static_cast<const int2*>(ctx->cells.p);
+  s.cell_tris = static_cast<const int*>(ctx->cell_tris.p);
+  s.reach = ctx->reach;
   return s;
 }
 }  // namespace linon
@@ -370,6 +413,8 @@ int linon_destroy(linon_ctx* ctx) {
   dev_free(ctx, ctx->scratch);
   dev_free(ctx, ctx->host_io);
   dev_free(ctx, ctx->grid);
+  dev_free(ctx, ctx->cells);
+  dev_free(ctx, ctx->cell_tris);
   linon::batch_release(ctx);
   if (ctx->d_err) cudaFree(ctx->d_err);
   for (cudaStream_t s : ctx->band_stream)
@@ -422,6 +467,8 @@ int linon_scene_upload(linon_ctx* ctx, const float* xyz, uint32_t n_vertices, co
   dev_free(ctx, ctx->scene_block);
   dev_free(ctx, ctx->face_rgb);
   dev_free(ctx, ctx->grid);
+  dev_free(ctx, ctx->cells);
+  dev_free(ctx, ctx->cell_tris);
   ctx->has_scene = false;
   if (int st = dev_alloc(ctx, ctx->scene_block, std::max<size_t>(bytes, 16))) return st;
   if (!b.nodes.empty())
@@ -447,6 +494,9 @@ int linon_scene_upload(linon_ctx* ctx, const float* xyz, uint32_t n_vertices, co
   // along the longest axis (at most 2^22 cells); skipped when the HBM budget
   // cannot hold it (the march then queries the BVH)
   dev_free(ctx, ctx->grid);
+  dev_free(ctx, ctx->cells);
+  dev_free(ctx, ctx->cell_tris);
+  ctx->reach = 0.0f;
   ctx->gx = ctx->gy = ctx->gz = 0;
   ctx->gcell = 0.0f;
   if (!b.nodes.empty()) {
@@ -479,6 +529,7 @@ int linon_scene_upload(linon_ctx* ctx, const float* xyz, uint32_t n_vertices, co
         const DevScene s = dev_scene(ctx);
         LINON_CUDA(launch_grid_build(s, static_cast<float*>(ctx->grid.p), ctx->stream));
         LINON_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (int st = build_cell_lists(ctx)) return st;
       }
     }
   }

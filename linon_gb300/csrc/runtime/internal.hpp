@@ -129,6 +129,9 @@ struct linon_ctx {
   linon::DevBuf grid;
   int gx = 0, gy = 0, gz = 0;
   float gox = 0.0f, goy = 0.0f, goz = 0.0f, gcell = 0.0f;
+  // per-cell candidate triangle lists of the segment test (empty: BVH only)
+  linon::DevBuf cells, cell_tris;
+  float reach = 0.0f;
   // device error word and scratch
   int* d_err = nullptr;
   linon::DevBuf scratch;       // grown on demand (capture positions, queues, ...)

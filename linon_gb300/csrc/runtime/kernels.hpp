@@ -31,6 +31,10 @@ struct FtleArgs {
 cudaError_t launch_overlay(const OverlayArgs& a, bool fp64, cudaStream_t s);
 // Fills the distance grid of s (s.gx * s.gy * s.gz floats) from its BVH.
 cudaError_t launch_grid_build(const DevScene& s, float* grid, cudaStream_t stream);
+// Candidate lists of the grid's cells: counts of the triangles in the leaves
+// within `reach` of each cell centre (-1 above max_list), then their slots.
+cudaError_t launch_cell_count(const DevScene& s, float reach, int max_list, int* counts, cudaStream_t stream);
+cudaError_t launch_cell_fill(const DevScene& s, float reach, const int2* lists, int* slots, cudaStream_t stream);
 cudaError_t launch_ftle(const FtleArgs& a, cudaStream_t s);
 // slots: 9 u64 (8 selection keys + a found counter)
 cudaError_t launch_outline(const float* e, int W, int H, float min_exp, unsigned long long* slots,
