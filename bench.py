@@ -419,7 +419,8 @@ def bench_batch(eng, stream, wl, torch, dev, predefined_source):
     return {"views": len(views), "rays": rays, "ray_steps": steps_batch, "plain_ms": plain_ms,
             "batched_ms": batch_ms, "plain_ray_steps_per_s": steps_plain / (plain_ms * 1e-3),
             "batched_ray_steps_per_s": steps_batch / (batch_ms * 1e-3), "speedup": plain_ms / batch_ms,
-            "tuning": {"quantum": tuning.quantum, "block_threads": tuning.block_threads,
+            "tuning": {"schedule": {1: "persistent queue", 2: "one CTA per tile"}.get(tuning.schedule, "auto"),
+                       "quantum": tuning.quantum, "block_threads": tuning.block_threads,
                        "tile": [tuning.tile_w, tuning.tile_h], "refill_below": tuning.refill_below}}
 
 

@@ -332,11 +332,14 @@ int linon_exponent_quantile(linon_ctx* ctx, const float* exponents,
  * Returns the number of u16 written, or a negative status.                */
 int linon_outline_indices(uint16_t* out, size_t cap);
 
-/* ---- batched rendering: many views in one persistent launch ------------
- * Views of any size, camera, step size and field go into one device work
- * queue of ray tiles; warps retire finished rays and refill their slots
- * from the queue every `quantum` steps.  fields[] may hold up to
- * LINON_MAX_BATCH_FIELDS distinct fields; views[i].field_index selects.    */
+/* ---- batched rendering: many views in one launch -----------------------
+ * Views of any size, camera, step size and field go into one launch, in
+ * one of two schedules: one CTA per 8x16-pixel tile of every view, views
+ * with the largest step budget first, the hardware balancing the CTAs (the
+ * default); or a persistent kernel over a device work queue of ray tiles
+ * whose warps retire finished rays and refill from the queue every
+ * `quantum` steps.  fields[] may hold up to LINON_MAX_BATCH_FIELDS
+ * distinct fields; views[i].field_index selects.                           */
 #define LINON_MAX_BATCH_FIELDS 8
 typedef struct linon_batch_tuning {
   int32_t quantum;          /* RK4 steps between retire/refill (0 = auto)  */
@@ -344,6 +347,9 @@ typedef struct linon_batch_tuning {
   int32_t ctas_per_sm;      /* resident CTAs per SM (0 = auto)             */
   int32_t tile_w, tile_h;   /* pixel tile handed out per queue pop (0=auto) */
   int32_t refill_below;     /* refill early when fewer lanes march (0=auto) */
+  int32_t schedule;         /* 0 auto (= 2), 1 persistent queue (the
+                               fields above), 2 one CTA per 8x16-pixel tile
+                               of every view (hardware scheduling)          */
 } linon_batch_tuning;
 int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields,
                        int32_t n_fields, const linon_view* views,

@@ -70,7 +70,8 @@ class View(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("quantum", C.c_int32), ("block_threads", C.c_int32), ("ctas_per_sm", C.c_int32),
-                ("tile_w", C.c_int32), ("tile_h", C.c_int32), ("refill_below", C.c_int32)]
+                ("tile_w", C.c_int32), ("tile_h", C.c_int32), ("refill_below", C.c_int32),
+                ("schedule", C.c_int32)]
 
 
 LINON_REQ_FRAME, LINON_REQ_OVERLAY, LINON_REQ_CAPTURE = 0, 1, 2

@@ -886,6 +886,67 @@ __device__ __forceinline__ void march_batch_kernel(const Fields& fields, const B
   }
 }
 
+// The other batched form: one launch, one 8 x 16-pixel CTA per tile of every
+// view (views' tiles concatenated, views with the largest step budget
+// first), the hardware's block scheduler balancing the load.  Each CTA's
+// view, march parameters and field are uniform; the march is the plain
+// kernel's (per-step warp vote, rays stop on their own budget or hit).
+__device__ __forceinline__ int find_view_block(const BatchArgs& a, int block) {
+  int lo = 0, hi = a.n_views - 1;  // last view with block_begin <= block
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (a.views[mid].block_begin <= block) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <int MODE = 0, class Fields>
+__device__ __forceinline__ void march_multi_kernel(const Fields& fields, const BatchArgs& a) {
+  extern __shared__ float4 linon_smem[];
+  __shared__ unsigned long long mbar;
+  const SceneView sc = cta_scene(a.scene, linon_smem, &mbar, a.err);
+  const int view = find_view_block(a, int(blockIdx.x));
+  const BatchView& V = a.views[view];
+  const int local = int(blockIdx.x) - V.block_begin;
+  const int x = (local % V.blocks_x) * 8 + int(threadIdx.x % 8);
+  const int row = (local / V.blocks_x) * 16 + int(threadIdx.x / 8);
+  const int W = V.frame.W, H = V.frame.H;
+  const bool in_image = x < W && row < H;
+  const DevMarch m = V.m;
+  const Basis b = make_basis(V.cam, W, H, m.focal_length, m.viewport_height);
+  const vec3f dir = primary_dir(b, in_image ? x : 0, in_image ? H - 1 - row : 0);
+  const size_t idx = in_image ? size_t(row) * W + x : 0;
+  RayState r;
+  ray_init(r, b.origin, dir, m.h_initial);
+  if (m.linear_mode) {
+    if (!in_image) return;
+    HitRec hit = intersect_segment<true>(sc, b.origin, dir, 100.0f, b.origin + 100.0f * dir, a.err);
+    wgsl::vec4f c(0.0f, 0.0f, 0.0f, 0.0f);
+    if (hit.t > 0.0f && hit.t < 100.0f) c = shade_hit(sc, hit, dir);
+    const DevFrame& out = V.frame;
+    if (out.color) {
+      uchar4 o;
+      o.x = unorm8(c.x); o.y = unorm8(c.y); o.z = unorm8(c.z); o.w = unorm8(c.w);
+      out.color[idx] = o;
+    }
+    if (out.hit) out.hit[idx] = hit.t > 0.0f && hit.t < 100.0f ? hit.id : -1;
+    if (out.mapping) out.mapping[idx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (out.steps) out.steps[idx] = 0;
+    return;
+  }
+  const FieldRef<Fields> field{fields, V.field};
+  bool active = in_image && ray_active(r, m);
+  while (__any_sync(0xffffffffu, active)) {
+    if (active) {
+      if (MODE == 0) ray_step_rt(r, field, m, sc, a.err);
+      else ray_step<false, MODE == 2, false, true>(r, field, m, sc, a.err);
+      active = ray_active(r, m);
+    }
+  }
+  if (in_image) ray_store(r, V.frame, idx);
+}
+
 // sample_rays generalised: one thread per ray; out[ray][point] float4.
 template <class F>
 __device__ __forceinline__ void capture_kernel(const F& field, const CaptureArgs& a) {

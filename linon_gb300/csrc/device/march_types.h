@@ -81,6 +81,8 @@ struct BatchView {
   int tiles_x;         // tiles per image row
   long long ray_begin; // first ray of this view in the batch's ray space
   DevFrame frame;
+  int block_begin;     // first CTA of this view in a one-CTA-per-tile launch
+  int blocks_x;        // 8 x 16-pixel CTA tiles per image row
 };
 
 struct BatchArgs {
@@ -92,7 +94,7 @@ struct BatchArgs {
   DevScene scene;
   int tile_w, tile_h;      // tile_w * tile_h == 32
   int refill_below;        // leave the quantum early below this many marching lanes
-  int pad;
+  int n_blocks;            // CTAs of a one-CTA-per-tile launch
   int* err;
 };
 

@@ -55,7 +55,13 @@ std::string batch_module_source(const std::vector<const linon_field*>& fields) {
        "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_batch_f(linon::BatchArgs a) {\n"
        "  linon::march_batch_kernel<1>(LinonFields(), a);\n}\n"
        "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_batch_fk(linon::BatchArgs a) {\n"
-       "  linon::march_batch_kernel<2>(LinonFields(), a);\n}\n";
+       "  linon::march_batch_kernel<2>(LinonFields(), a);\n}\n"
+       "extern \"C\" __global__ void __launch_bounds__(128) linon_multi(linon::BatchArgs a) {\n"
+       "  linon::march_multi_kernel<0>(LinonFields(), a);\n}\n"
+       "extern \"C\" __global__ void __launch_bounds__(128) linon_multi_f(linon::BatchArgs a) {\n"
+       "  linon::march_multi_kernel<1>(LinonFields(), a);\n}\n"
+       "extern \"C\" __global__ void __launch_bounds__(128) linon_multi_fk(linon::BatchArgs a) {\n"
+       "  linon::march_multi_kernel<2>(LinonFields(), a);\n}\n";
   return s.str();
 }
 
@@ -88,7 +94,10 @@ int get_module(linon_ctx* ctx, BatchState& bs, const linon_field* const* fields,
   }
   std::string log;
   const bool precise = (fv[0]->flags & LINON_COMPILE_PRECISE) != 0;
-  int st = jit_compile(batch_module_source(fv), precise, {"linon_batch", "linon_batch_f", "linon_batch_fk"}, mod, log);
+  int st = jit_compile(batch_module_source(fv), precise,
+                       {"linon_batch", "linon_batch_f", "linon_batch_fk", "linon_multi", "linon_multi_f",
+                        "linon_multi_fk"},
+                       mod, log);
   if (st != LINON_OK) return set_error(st, st == LINON_ECOMPILE ? log : std::string(linon_last_error()));
   bs.modules[key] = mod;
   (void)ctx;
@@ -152,6 +161,10 @@ int batch_tuning(const linon_ctx* ctx, const linon_batch_tuning* in, linon_batch
   else if (ctx->has_tuned) t = ctx->tuned;
   // default: refill a warp when all its lanes are done (see the autotuner)
   if (t.quantum <= 0) t.quantum = 1024;
+  if (t.schedule < 0 || t.schedule > 2) return set_error(LINON_EINVAL, "schedule must be 0, 1 or 2");
+  // auto: one CTA per tile (64 uneven views: 16.4 ms against 20.1 ms for
+  // the best persistent-queue tuning)
+  if (t.schedule == 0) t.schedule = 2;
   // 0: refill only at the end of a quantum (measured best on the 64-view
   // workload: an early refill costs a queue atomic and a camera set-up)
   if (t.refill_below < 0) t.refill_below = 0;
@@ -168,7 +181,7 @@ int batch_tuning(const linon_ctx* ctx, const linon_batch_tuning* in, linon_batch
 }
 
 long long batch_table(const linon_view* views, int n_views, const linon_batch_tuning& t,
-                      std::vector<BatchView>& tab) {
+                      std::vector<BatchView>& tab, int* n_blocks) {
   tab.assign(static_cast<size_t>(n_views), BatchView());
   // Queue order: views with the largest step budget per ray first, so that
   // when the queue drains the SMs finish on short rays (longest-first list
@@ -183,10 +196,14 @@ long long batch_table(const linon_view* views, int n_views, const linon_batch_tu
   }
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return budget[size_t(a)] > budget[size_t(b)]; });
   long long begin = 0;
+  int blocks = 0;
   for (int k = 0; k < n_views; ++k) {
     const int i = order[size_t(k)];
     const linon_view& v = views[i];
     BatchView& b = tab[size_t(k)];
+    b.block_begin = blocks;
+    b.blocks_x = (v.width + 7) / 8;
+    blocks += b.blocks_x * ((v.height + 15) / 16);
     b.m = to_dev(v.settings, v.params);
     for (int k = 0; k < 3; ++k) {
       b.cam.o[k] = v.camera.origin[k];
@@ -205,6 +222,7 @@ long long batch_table(const linon_view* views, int n_views, const linon_batch_tu
     b.frame.steps = v.out.steps;
     begin += (long long)b.tiles_x * tiles_y * 32;
   }
+  if (n_blocks) *n_blocks = blocks;
   return begin;
 }
 
@@ -214,18 +232,20 @@ int batch_module(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fie
   return get_module(ctx, g_batch[ctx], fields, n_fields, mod);
 }
 
-const char* batch_kernel_name(const linon_view* views, int n_views) {
+const char* batch_kernel_name(const linon_view* views, int n_views, int schedule) {
+  const bool multi = schedule == 2;
   bool kahan = false, plain = false;
   for (int i = 0; i < n_views; ++i) {
-    if (views[i].params.adaptive) return "linon_batch";
+    if (views[i].params.adaptive) return multi ? "linon_multi" : "linon_batch";
     (views[i].params.kahan ? kahan : plain) = true;
   }
-  if (kahan && plain) return "linon_batch";
+  if (kahan && plain) return multi ? "linon_multi" : "linon_batch";
+  if (multi) return kahan ? "linon_multi_fk" : "linon_multi_f";
   return kahan ? "linon_batch_fk" : "linon_batch_f";
 }
 
 int batch_launch(linon_ctx* ctx, const std::shared_ptr<JitModule>& mod, const linon_batch_tuning& t,
-                 const BatchView* views_dev, int n_views, long long total_rays,
+                 const BatchView* views_dev, int n_views, long long total_rays, int n_blocks,
                  unsigned long long* counter, cudaStream_t stream, const char* kernel) {
   BatchArgs a;
   std::memset(&a, 0, sizeof a);
@@ -238,8 +258,16 @@ int batch_launch(linon_ctx* ctx, const std::shared_ptr<JitModule>& mod, const li
   a.tile_w = t.tile_w;
   a.tile_h = t.tile_h;
   a.refill_below = t.refill_below;
+  a.n_blocks = n_blocks;
   a.err = ctx->d_err;
   cudaKernel_t k = mod->kernels.at(kernel);
+  if (t.schedule == 2) {
+    if (n_blocks <= 0) return LINON_OK;
+    void* args[] = {&a};
+    LINON_CUDA(cudaLaunchKernel((const void*)k, dim3(unsigned(n_blocks)), dim3(128), args,
+                                size_t(a.scene.staged_bytes), stream));
+    return LINON_OK;
+  }
   int sms = 0;
   LINON_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   int per_sm = t.ctas_per_sm;
@@ -286,7 +314,8 @@ int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields, int32_t
     linon_batch_tuning t;
     if (int st = batch_tuning(ctx, tuning, t)) return st;
     std::vector<BatchView> tab;
-    const long long begin = batch_table(views, n_views, t, tab);
+    int n_blocks = 0;
+    const long long begin = batch_table(views, n_views, t, tab, &n_blocks);
     if (int st = dev_grow(ctx, bs.views, sizeof(BatchView) * tab.size())) return st;
     if (int st = dev_grow(ctx, bs.counter, 256)) return st;
     LINON_CUDA(cudaMemcpyAsync(bs.views.p, tab.data(), sizeof(BatchView) * tab.size(),
@@ -302,18 +331,26 @@ int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields, int32_t
     a.tile_w = t.tile_w;
     a.tile_h = t.tile_h;
     a.refill_below = t.refill_below;
+    a.n_blocks = n_blocks;
     a.err = ctx->d_err;
-    cudaKernel_t k = mod->kernels.at(batch_kernel_name(views, n_views));
-    int sms = 0;
-    LINON_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
-    int per_sm = t.ctas_per_sm;
-    if (per_sm <= 0) {
-      int occ = 0;
-      LINON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)k, t.block_threads,
-                                                               size_t(a.scene.staged_bytes)));
-      per_sm = std::max(1, occ);
+    cudaKernel_t k = mod->kernels.at(batch_kernel_name(views, n_views, t.schedule));
+    dim3 grid, block;
+    if (t.schedule == 2) {
+      grid = dim3(unsigned(std::max(n_blocks, 1)));
+      block = dim3(128);
+    } else {
+      int sms = 0;
+      LINON_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+      int per_sm = t.ctas_per_sm;
+      if (per_sm <= 0) {
+        int occ = 0;
+        LINON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)k, t.block_threads,
+                                                                 size_t(a.scene.staged_bytes)));
+        per_sm = std::max(1, occ);
+      }
+      grid = dim3(unsigned(sms * per_sm));
+      block = dim3(unsigned(t.block_threads));
     }
-    const dim3 grid(unsigned(sms * per_sm)), block(unsigned(t.block_threads));
     // graph key: the kernel parameters and the launch shape
     std::vector<char> key(sizeof a + sizeof(k) + 2 * sizeof(unsigned));
     std::memcpy(key.data(), &a, sizeof a);
@@ -378,6 +415,7 @@ int linon_autotune_batch(linon_ctx* ctx, const linon_field* const* fields, int32
       for (auto& tl : tiles)
         for (int rf : refills) {
         linon_batch_tuning t{};
+        t.schedule = 1;
         t.quantum = q;
         t.block_threads = b;
         t.tile_w = tl[0];
@@ -404,6 +442,29 @@ int linon_autotune_batch(linon_ctx* ctx, const linon_field* const* fields, int32
           bt = t;
         }
       }
+  {
+    // the one-CTA-per-tile launch
+    linon_batch_tuning t{};
+    t.schedule = 2;
+    int st = linon_render_batch(ctx, fields, n_fields, views, n_views, &t);
+    if (!st) {
+      cudaEventRecord(e0, ctx->stream);
+      st = linon_render_batch(ctx, fields, n_fields, views, n_views, &t);
+      cudaEventRecord(e1, ctx->stream);
+    }
+    if (st) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return st;
+    }
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_t) {
+      best_t = ms;
+      bt = t;
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   ctx->tuned = bt;

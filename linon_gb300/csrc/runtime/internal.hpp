@@ -87,15 +87,15 @@ void batch_release(linon_ctx* ctx);
 // Pieces of the batched launch, shared with the serving loop (batch.cpp).
 int batch_tuning(const linon_ctx* ctx, const linon_batch_tuning* in, linon_batch_tuning& t);
 long long batch_table(const linon_view* views, int n_views, const linon_batch_tuning& t,
-                      std::vector<BatchView>& tab);
+                      std::vector<BatchView>& tab, int* n_blocks = nullptr);
 int batch_module(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fields,
                  std::shared_ptr<JitModule>& mod);
 // The batched kernel for a set of views: linon_batch_f / linon_batch_fk when
 // no view refines its step adaptively and all (or none) use Kahan sums,
 // otherwise the generic linon_batch.
-const char* batch_kernel_name(const linon_view* views, int n_views);
+const char* batch_kernel_name(const linon_view* views, int n_views, int schedule);
 int batch_launch(linon_ctx* ctx, const std::shared_ptr<JitModule>& mod, const linon_batch_tuning& t,
-                 const BatchView* views_dev, int n_views, long long total_rays,
+                 const BatchView* views_dev, int n_views, long long total_rays, int n_blocks,
                  unsigned long long* counter, cudaStream_t stream, const char* kernel);
 
 }  // namespace linon

@@ -212,11 +212,12 @@ int launch_wave(linon_server* s, Slot& sl) {
   }
   if (!views.empty()) {
     std::vector<BatchView> tab;
-    const long long total = batch_table(views.data(), int(views.size()), s->tuning, tab);
+    int n_blocks = 0;
+    const long long total = batch_table(views.data(), int(views.size()), s->tuning, tab, &n_blocks);
     LINON_CUDA(cudaMemcpyAsync(sl.views_dev, tab.data(), sizeof(BatchView) * tab.size(), cudaMemcpyHostToDevice,
                                sl.main));
-    if (int st = batch_launch(ctx, s->mod, s->tuning, sl.views_dev, int(views.size()), total, sl.counter, sl.main,
-                              batch_kernel_name(views.data(), int(views.size()))))
+    if (int st = batch_launch(ctx, s->mod, s->tuning, sl.views_dev, int(views.size()), total, n_blocks, sl.counter,
+                              sl.main, batch_kernel_name(views.data(), int(views.size()), s->tuning.schedule)))
       return st;
     for (size_t i = 0; i < renders.size(); ++i) {
       Request* q = renders[i];

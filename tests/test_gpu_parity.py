@@ -449,14 +449,18 @@ def snapshot(planes):
 
 
 @pytest.mark.parametrize("precise", [True, False])
-def test_batch_equals_plain(engine, precise):
+@pytest.mark.parametrize("schedule", [1, 2])
+def test_batch_equals_plain(engine, precise, schedule):
+    """Both batched forms (1: persistent queue with mid-ray refills, a small
+    quantum; 2: one CTA per tile of every view) against one plain launch per
+    view."""
     flds, views, planes = batch_setup(engine, precise)
     engine.render_views_plain(flds, views)
     a = snapshot(planes)
     for p in planes:
         for k in ("color", "mapping", "hit_id", "steps"):
             getattr(p, k).zero_()
-    tuning = _abi.BatchTuning(16, 64, 0, 8, 4)
+    tuning = _abi.BatchTuning(16, 64, 0, 8, 4, 0, schedule)
     engine.render_batch(flds, views, tuning)
     engine.synchronize()
     b = snapshot(planes)
@@ -497,12 +501,17 @@ def test_batch_graph_replay_and_tuning(engine):
         for k in x:
             np.testing.assert_array_equal(x[k], y[k])
     t, ms = engine.autotune_batch(flds, views)
-    assert t.quantum in (256, 1024, 4096) and t.refill_below in (0, 8) and ms > 0
-    # the tuned launch gives the same planes as the default one
+    assert ms > 0 and (t.schedule == 2 or (t.schedule == 1 and t.quantum in (256, 1024, 4096)
+                                           and t.refill_below in (0, 8)))
+    # the tuned launch gives the default one's planes (fast modules: the two
+    # batched kernels may contract FMAs differently, so to FP32 tolerance)
     engine.render_batch(flds, views, t)
     for x, y in zip(first, snapshot(planes)):
-        for k in x:
-            np.testing.assert_array_equal(x[k], y[k])
+        assert np.mean(x["hit_id"] != y["hit_id"]) <= 0.005
+        same = (x["hit_id"] == y["hit_id"]) & (x["steps"] == y["steps"])
+        assert same.mean() >= 0.99
+        d = np.abs(x["mapping"] - y["mapping"]).max(axis=-1)
+        assert np.percentile(d[same], 99) <= 1e-4
 
 
 def test_hbm_budget_admission():
