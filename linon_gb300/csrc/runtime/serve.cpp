@@ -11,8 +11,8 @@
 //     fits the HBM budget (outputs come from the stream-ordered pool);
 //   * each admitted group (a wave) goes to a free slot (a pair of streams):
 //     frames / Enhance re-renders / overlay renders of the wave in ONE
-//     persistent batched launch, then the overlays, while captures run on the
-//     slot's second stream;
+//     batched launch (the configured schedule), then the overlays, while
+//     captures run on the slot's second stream;
 //   * up to `slots` waves are on the GPU at once, so requests that arrive
 //     while a wave runs start in the next slot without waiting for it;
 //   * completion is detected by polling the waves' events; results stay on
