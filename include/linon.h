@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define LINON_ABI_VERSION 1
+#define LINON_ABI_VERSION 2  /* 2: linon_batch_tuning.schedule */
 
 /* ---- status codes ------------------------------------------------------ */
 enum linon_status {

@@ -166,6 +166,7 @@ PROTOTYPES = {
 }
 
 _lib = None
+ABI_VERSION = 2  # include/linon.h LINON_ABI_VERSION (struct layouts of this file)
 
 
 def load(path: str | os.PathLike | None = None) -> C.CDLL:
@@ -182,6 +183,9 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
+    if lib.linon_abi_version() != ABI_VERSION:
+        raise RuntimeError(f"{p}: ABI version {lib.linon_abi_version()}, these bindings expect {ABI_VERSION} "
+                           "(rebuild with python -m linon_gb300.build)")
     if path is None:
         _lib = lib
     return lib

@@ -44,7 +44,7 @@ def test_reference_params(lib):
 
 
 def test_status_strings_and_predefined(lib):
-    assert lib.linon_abi_version() == 1
+    assert lib.linon_abi_version() == 2
     assert lib.linon_status_string(_abi.LINON_ECOMPILE) == b"field function compilation failed"
     assert predefined_name(3) == "Mirage (spherical sigmoid)"
     assert predefined_name(9) == "Roessler attractor"
