@@ -125,6 +125,15 @@ __device__ __forceinline__ bool box_overlap(const float4& lo, const float4& hi, 
 #define LINON_BATCH_BOUNDS __launch_bounds__(256)
 #endif
 
+// Launch bounds of the one-CTA-per-tile batched kernels: 128-thread CTAs,
+// at least LINON_MULTI_MIN_CTAS (default 8) resident per SM, which caps them
+// at 64 registers (64 uneven views: 16.5 ms uncapped at 72 registers, 14.8
+// ms at 8 or 9 CTAs per SM, 15.6 ms at 10, 16.2 ms at 12).
+#ifndef LINON_MULTI_MIN_CTAS
+#define LINON_MULTI_MIN_CTAS 8
+#endif
+#define LINON_MULTI_BOUNDS __launch_bounds__(128, LINON_MULTI_MIN_CTAS)
+
 // Launch bounds of the plain march kernels (128-thread CTAs).  Defining
 // LINON_MARCH_MIN_CTAS adds the minimum resident CTAs per SM, which caps the
 // registers per thread (and may spill).

@@ -9,6 +9,7 @@
 // quantum x block size x tile shape on the caller's batch and caches the
 // winner in the context.
 #include <algorithm>
+#include <cstdlib>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -56,11 +57,11 @@ std::string batch_module_source(const std::vector<const linon_field*>& fields) {
        "  linon::march_batch_kernel<1>(LinonFields(), a);\n}\n"
        "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_batch_fk(linon::BatchArgs a) {\n"
        "  linon::march_batch_kernel<2>(LinonFields(), a);\n}\n"
-       "extern \"C\" __global__ void __launch_bounds__(128) linon_multi(linon::BatchArgs a) {\n"
+       "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_multi(linon::BatchArgs a) {\n"
        "  linon::march_multi_kernel<0>(LinonFields(), a);\n}\n"
-       "extern \"C\" __global__ void __launch_bounds__(128) linon_multi_f(linon::BatchArgs a) {\n"
+       "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_multi_f(linon::BatchArgs a) {\n"
        "  linon::march_multi_kernel<1>(LinonFields(), a);\n}\n"
-       "extern \"C\" __global__ void __launch_bounds__(128) linon_multi_fk(linon::BatchArgs a) {\n"
+       "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_multi_fk(linon::BatchArgs a) {\n"
        "  linon::march_multi_kernel<2>(LinonFields(), a);\n}\n";
   return s.str();
 }
@@ -87,6 +88,8 @@ int get_module(linon_ctx* ctx, BatchState& bs, const linon_field* const* fields,
   std::vector<const linon_field*> fv(fields, fields + n_fields);
   std::string key;
   for (auto* f : fv) key += f->cuda + "\x01" + std::to_string(f->flags) + "\x02";
+  // the extra compiler options are part of what the module is
+  if (const char* extra = std::getenv("LINON_JIT_OPTIONS")) key += extra;
   auto it = bs.modules.find(key);
   if (it != bs.modules.end()) {
     mod = it->second;
