@@ -10,8 +10,9 @@
 //   :281-314 sample_rays, :470-479 capture seeds
 // Every arithmetic expression keeps the shader's evaluation order, so a
 // module compiled with LINON_PRECISE and --fmad=false is op-for-op the FP32
-// restatement.  Fast modules let the compiler contract a*b+c into FMA and use
-// the hardware reciprocal square root.
+// restatement.  Fast modules let the compiler contract a*b+c into FMA, issue
+// the march's float3 arithmetic as packed FP32 pairs (wgsl_rt.cuh vmadd &c.)
+// and use the hardware reciprocal square root.
 #pragma once
 
 #include "wgsl_rt.cuh"
@@ -20,12 +21,6 @@
 namespace linon {
 
 using wgsl::vec3f;
-
-#if defined(LINON_PRECISE)
-#define LINON_DIV6(x) ((x) / 6.0f)
-#else
-#define LINON_DIV6(x) ((x) * (1.0f / 6.0f))
-#endif
 
 // --------------------------------------------------------------------------
 // Scene access.  Triangles are four float4 each: (v0, face id bits),
@@ -471,6 +466,24 @@ __device__ __forceinline__ void kahan_add(float& sum, float& c, float x) {
   c = (t - sum) - y;
   sum = t;
 }
+// kahan_add on each component (packed x/y pairs in fast modules)
+__device__ __forceinline__ void kahan_add3(vec3f& sum, vec3f& c, const vec3f& x) {
+  const vec3f y = wgsl::vsub(x, c);
+  const vec3f t = wgsl::vadd(sum, y);
+  c = wgsl::vsub(wgsl::vsub(t, sum), y);
+  sum = t;
+}
+
+// (((k1 + 2 k2) + 2 k3) + k4) / 6, the RK4 average in the shader's order
+__device__ __forceinline__ vec3f rk4_combine(const vec3f& k1, const vec3f& k2, const vec3f& k3,
+                                             const vec3f& k4) {
+  const vec3f s = wgsl::vadd(wgsl::vmadd(k3, 2.0f, wgsl::vmadd(k2, 2.0f, k1)), k4);
+#if defined(LINON_PRECISE)
+  return s / 6.0f;
+#else
+  return wgsl::vscale(s, 1.0f / 6.0f);
+#endif
+}
 
 // Is the ray still marching?  (loop condition of main_view.wgsl:244, or the
 // fixed step budget, or the first hit with stop_on_hit)
@@ -501,10 +514,10 @@ __device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevM
   const float h = r.h;
   const float hh = 0.5f * h;
   const vec3f k1 = field(r.p, r.p, r.v0, r.dir, r.t);
-  const vec3f k2 = field(r.p, r.p + hh * k1, r.v0, k1, r.t + hh);
-  const vec3f k3 = field(r.p, r.p + hh * k2, r.v0, k2, r.t + hh);
-  const vec3f k4 = field(r.p, r.p + h * k3, r.v0, k3, r.t + h);
-  const vec3f v = LINON_DIV6(((k1 + 2.0f * k2) + 2.0f * k3) + k4);
+  const vec3f k2 = field(r.p, wgsl::vmadd(k1, hh, r.p), r.v0, k1, r.t + hh);
+  const vec3f k3 = field(r.p, wgsl::vmadd(k2, hh, r.p), r.v0, k2, r.t + hh);
+  const vec3f k4 = field(r.p, wgsl::vmadd(k3, h, r.p), r.v0, k3, r.t + h);
+  const vec3f v = rk4_combine(k1, k2, k3, k4);
   float diff = 0.0f;
   if (ADAPTIVE) {
     diff = wgsl::length(v - r.last_v);
@@ -517,17 +530,17 @@ __device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevM
     r.dir = v;
   } else {
     const float w = m.field_weight;
-    r.dir = (1.0f - w) * r.dir + w * v;
+    r.dir = wgsl::vmadd(v, w, (1.0f - w) * r.dir);
   }
-  const vec3f step_dir = r.dir * h;
+  const vec3f step_dir = wgsl::vscale(r.dir, h);
   if (!r.has_color) {
     // Safe-ball skip (BVH scenes): every point within the ball of radius
     // sqrt(safe2) around q0 is farther than the culling margin from every
     // triangle, and a segment whose ends both lie in the ball lies in it
     // (the ball is convex; the start was checked by the previous step), so
     // such a segment cannot hit anything the brute-force loop would hit.
-    const vec3f seg_end = r.p + step_dir;
-    const vec3f dq = seg_end - r.q0;
+    const vec3f seg_end = wgsl::vadd(r.p, step_dir);
+    const vec3f dq = wgsl::vsub(seg_end, r.q0);
     if (!(sc.n_nodes > 0 && wgsl::dot(dq, dq) <= r.safe2)) {
       const float len = wgsl::length(step_dir);
 #if defined(LINON_PRECISE)
@@ -557,12 +570,10 @@ __device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevM
     }
   }
   if (KAHAN) {
-    kahan_add(r.p.x, r.cp.x, step_dir.x);
-    kahan_add(r.p.y, r.cp.y, step_dir.y);
-    kahan_add(r.p.z, r.cp.z, step_dir.z);
+    kahan_add3(r.p, r.cp, step_dir);
     kahan_add(r.t, r.ct, h);
   } else {
-    r.p = r.p + step_dir;
+    r.p = wgsl::vadd(r.p, step_dir);
     r.t = r.t + h;
   }
   if (ADAPTIVE) {
@@ -969,14 +980,14 @@ __device__ __forceinline__ void capture_kernel(const F& field, const CaptureArgs
   float4* out = a.out + size_t(ray) * a.n_points;
   for (int i = 0; i < a.n_steps; ++i) {
     const vec3f k1 = field(p, p, start_dir, dir, t);
-    const vec3f k2 = field(p, p + hh * k1, start_dir, k1, t + hh);
-    const vec3f k3 = field(p, p + hh * k2, start_dir, k2, t + hh);
-    const vec3f k4 = field(p, p + h * k3, start_dir, k3, t + h);
-    const vec3f v = LINON_DIV6(((k1 + 2.0f * k2) + 2.0f * k3) + k4);
-    dir = (1.0f - w) * dir + w * v;
-    const vec3f step_dir = dir * h;
+    const vec3f k2 = field(p, wgsl::vmadd(k1, hh, p), start_dir, k1, t + hh);
+    const vec3f k3 = field(p, wgsl::vmadd(k2, hh, p), start_dir, k2, t + hh);
+    const vec3f k4 = field(p, wgsl::vmadd(k3, h, p), start_dir, k3, t + h);
+    const vec3f v = rk4_combine(k1, k2, k3, k4);
+    dir = wgsl::vmadd(v, w, (1.0f - w) * dir);
+    const vec3f step_dir = wgsl::vscale(dir, h);
     if (i % a.every == 0) out[i / a.every] = make_float4(p.x, p.y, p.z, 1.0f);
-    p = p + step_dir;
+    p = wgsl::vadd(p, step_dir);
     t = t + h;
   }
   if (a.record_final) out[a.n_points - 1] = make_float4(p.x, p.y, p.z, 1.0f);

@@ -583,6 +583,65 @@ template <int N> WG_HD float distance(const vec<float, N>& a, const vec<float, N
   return length(a - b);
 }
 WG_HD float distance(float a, float b) { return fabsf(a - b); }
+// ---------------------------------------------------------------------------
+// Fused float3 operations for the march (c + s * a and friends).  Fast
+// modules on sm_100 and later issue the x and y components as one packed
+// FP32 pair operation (f32x2: two results per issued instruction, each
+// rounded exactly like the scalar operation) and z as a scalar one; the
+// march is issue-bound, so this removes issue slots without changing any
+// rounding.  Precise modules and the host evaluate the shader's separate
+// multiply and add.  LINON_NO_F32X2 turns the packing off.
+// ---------------------------------------------------------------------------
+#if defined(__CUDA_ARCH__) && !defined(LINON_PRECISE) && !defined(LINON_NO_F32X2)
+#if __CUDA_ARCH__ >= 1000
+#define LINON_F32X2 1
+#endif
+#endif
+#ifdef LINON_F32X2
+WG_HD float2 xy2(const vec3f& a) { return make_float2(a.x, a.y); }
+#endif
+// c + s * a
+WG_HD vec3f vmadd(const vec3f& a, float s, const vec3f& c) {
+#ifdef LINON_F32X2
+  const float2 r = __ffma2_rn(xy2(a), make_float2(s, s), xy2(c));
+  return vec3f(r.x, r.y, fmaf(a.z, s, c.z));
+#else
+  return c + s * a;
+#endif
+}
+// a * s
+WG_HD vec3f vscale(const vec3f& a, float s) {
+#ifdef LINON_F32X2
+  const float2 r = __fmul2_rn(xy2(a), make_float2(s, s));
+  return vec3f(r.x, r.y, a.z * s);
+#else
+  return a * s;
+#endif
+}
+// a + b
+WG_HD vec3f vadd(const vec3f& a, const vec3f& b) {
+#ifdef LINON_F32X2
+  const float2 r = __fadd2_rn(xy2(a), xy2(b));
+  return vec3f(r.x, r.y, a.z + b.z);
+#else
+  return a + b;
+#endif
+}
+// a - b (PTX sub.rn.f32x2; there is no packed-subtract builtin)
+WG_HD vec3f vsub(const vec3f& a, const vec3f& b) {
+#ifdef LINON_F32X2
+  unsigned long long pa, pb, pd;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(pa) : "f"(a.x), "f"(a.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(pb) : "f"(b.x), "f"(b.y));
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(pd) : "l"(pa), "l"(pb));
+  float rx, ry;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(rx), "=f"(ry) : "l"(pd));
+  return vec3f(rx, ry, a.z - b.z);
+#else
+  return a - b;
+#endif
+}
+
 template <int N> WG_HD vec<float, N> normalize(const vec<float, N>& v) {
 #if defined(LINON_PRECISE) || !defined(__CUDA_ARCH__)
   float l = sqrtf(dot(v, v));
@@ -591,6 +650,13 @@ template <int N> WG_HD vec<float, N> normalize(const vec<float, N>& v) {
   return v * rsqrtf(dot(v, v));
 #endif
 }
+// LINON_PACKED_NORMALIZE: fast float3 normalize scales x/y as one packed
+// pair (the scale factor has to be paired first; whether that pays depends
+// on the kernel's register allocation, so the module that includes this
+// file decides).
+#if defined(LINON_F32X2) && defined(LINON_PACKED_NORMALIZE)
+template <> WG_HD vec3f normalize<3>(const vec3f& v) { return vscale(v, rsqrtf(dot(v, v))); }
+#endif
 // reflect(e1, e2) = e1 - 2 * dot(e2, e1) * e2
 template <int N> WG_HD vec<float, N> reflect(const vec<float, N>& e1, const vec<float, N>& e2) {
   float d = 2.0f * dot(e2, e1);
