@@ -43,13 +43,26 @@ std::string batch_module_source(const std::vector<const linon_field*>& fields) {
     if (p != std::string::npos) code.replace(p, from.size(), "namespace linon_user_" + std::to_string(i) + " {");
     s << code;
   }
+  // one functor per field, and LinonFields: field i chosen per call (the
+  // persistent kernels, whose warps mix views) or once per CTA by visit()
+  // (the one-CTA-per-tile kernels, whose CTAs lie in one view)
+  for (size_t i = 0; i < fields.size(); ++i)
+    s << "struct LinonField" << i << " {\n"
+         "  __device__ __forceinline__ wgsl::vec3f operator()(const wgsl::vec3f& pp, const wgsl::vec3f& p,\n"
+         "      const wgsl::vec3f& v0, const wgsl::vec3f& v, float t) const {\n"
+         "    return linon_user_" << i << "::field_function(pp, p, v0, v, t);\n  }\n};\n";
   s << "struct LinonFields {\n"
        "  __device__ __forceinline__ wgsl::vec3f operator()(int i, const wgsl::vec3f& pp, const wgsl::vec3f& p,\n"
        "      const wgsl::vec3f& v0, const wgsl::vec3f& v, float t) const {\n"
        "    switch (i) {\n";
   for (size_t i = 1; i < fields.size(); ++i)
-    s << "      case " << i << ": return linon_user_" << i << "::field_function(pp, p, v0, v, t);\n";
-  s << "      default: return linon_user_0::field_function(pp, p, v0, v, t);\n"
+    s << "      case " << i << ": return LinonField" << i << "()(pp, p, v0, v, t);\n";
+  s << "      default: return LinonField0()(pp, p, v0, v, t);\n"
+       "    }\n  }\n"
+       "  template <class Fn> __device__ __forceinline__ void visit(int i, const Fn& fn) const {\n"
+       "    switch (i) {\n";
+  for (size_t i = 1; i < fields.size(); ++i) s << "      case " << i << ": fn(LinonField" << i << "()); return;\n";
+  s << "      default: fn(LinonField0()); return;\n"
        "    }\n  }\n};\n"
        "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_batch(linon::BatchArgs a) {\n"
        "  linon::march_batch_kernel<0>(LinonFields(), a);\n}\n"
