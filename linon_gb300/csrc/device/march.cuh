@@ -514,9 +514,12 @@ __device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevM
   const float h = r.h;
   const float hh = 0.5f * h;
   const vec3f k1 = field(r.p, r.p, r.v0, r.dir, r.t);
-  const vec3f k2 = field(r.p, wgsl::vmadd(k1, hh, r.p), r.v0, k1, r.t + hh);
-  const vec3f k3 = field(r.p, wgsl::vmadd(k2, hh, r.p), r.v0, k2, r.t + hh);
-  const vec3f k4 = field(r.p, wgsl::vmadd(k3, h, r.p), r.v0, k3, r.t + h);
+  // The stage positions stay scalar (FMA-contracted) so that the compiler
+  // drops the components a field never reads (the three 1080p frames: 62.2
+  // ms scalar, 62.9 ms packed).
+  const vec3f k2 = field(r.p, r.p + hh * k1, r.v0, k1, r.t + hh);
+  const vec3f k3 = field(r.p, r.p + hh * k2, r.v0, k2, r.t + hh);
+  const vec3f k4 = field(r.p, r.p + h * k3, r.v0, k3, r.t + h);
   const vec3f v = rk4_combine(k1, k2, k3, k4);
   float diff = 0.0f;
   if (ADAPTIVE) {
@@ -984,9 +987,9 @@ __device__ __forceinline__ void capture_kernel(const F& field, const CaptureArgs
   float4* out = a.out + size_t(ray) * a.n_points;
   for (int i = 0; i < a.n_steps; ++i) {
     const vec3f k1 = field(p, p, start_dir, dir, t);
-    const vec3f k2 = field(p, wgsl::vmadd(k1, hh, p), start_dir, k1, t + hh);
-    const vec3f k3 = field(p, wgsl::vmadd(k2, hh, p), start_dir, k2, t + hh);
-    const vec3f k4 = field(p, wgsl::vmadd(k3, h, p), start_dir, k3, t + h);
+    const vec3f k2 = field(p, p + hh * k1, start_dir, k1, t + hh);
+    const vec3f k3 = field(p, p + hh * k2, start_dir, k2, t + hh);
+    const vec3f k4 = field(p, p + h * k3, start_dir, k3, t + h);
     const vec3f v = rk4_combine(k1, k2, k3, k4);
     dir = wgsl::vmadd(v, w, (1.0f - w) * dir);
     const vec3f step_dir = wgsl::vscale(dir, h);
