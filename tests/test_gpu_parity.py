@@ -478,6 +478,44 @@ def test_batch_equals_plain(engine, precise, schedule):
             assert np.percentile(d[same], 99) <= 1e-4
 
 
+@pytest.mark.parametrize("schedule", [1, 2])
+def test_batch_eight_fields_equals_plain(engine, schedule):
+    """The most fields one batch takes (LINON_MAX_BATCH_FIELDS = 8), one view
+    per field plus two more: the per-CTA field choice of the tile schedule
+    (one march loop per field) and the per-ray choice of the persistent
+    queue each pick the right field.  Precise modules, bit-exact against one
+    plain launch per view."""
+    xyz, faces, rgb = scene.cornell_with_spheres(seed=2, subdivisions=1)
+    engine.upload_scene(xyz, faces, rgb, bvh=True)
+    # (no "identity": it returns v, which equals linear's v0 on straight rays)
+    names = ["linear", "twist", "lens", "lorenz_scaled", "mirage_spherical", "rotation",
+             "translation_x", "mirage_plane"]
+    assert len(names) == _abi.LINON_MAX_BATCH_FIELDS
+    flds = [field(engine, nme, True) for nme in names]
+    views, planes = [], []
+    specs = wl.batch_views(10, seed=11, min_side=20, max_side=70, n_fields=8)
+    for i, (W, H, camera, params, fidx) in enumerate(specs):
+        params.max_steps = min(params.max_steps, 120)
+        fp = FramePlanes.allocate(W, H)
+        v = _abi.View()
+        v.camera, v.settings, v.params = camera, wl.settings(), params
+        v.width, v.height = W, H
+        v.field_index = i if i < 8 else fidx  # every field at least once
+        v.out = fp.abi()
+        views.append(v)
+        planes.append(fp)
+    engine.render_views_plain(flds, views)
+    a = snapshot(planes)
+    for p in planes:
+        for k in ("color", "mapping", "hit_id", "steps"):
+            getattr(p, k).zero_()
+    engine.render_batch(flds, views, _abi.BatchTuning(16, 64, 0, 8, 4, 0, schedule))
+    engine.synchronize()
+    for x, y in zip(a, snapshot(planes)):
+        for k in x:
+            np.testing.assert_array_equal(x[k], y[k])
+
+
 def test_batch_alone_equals_in_mix(engine):
     flds, views, planes = batch_setup(engine, True, n=5)
     engine.render_batch(flds, views[:1])
