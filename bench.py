@@ -152,6 +152,63 @@ def cpu_baseline(pyoracle, w, budget_s=12.0):
     return steps / dt, threads, f"{n} of {n_total} pixels (uniform random, seed 0) x {len(w.fields)} fields, {dt:.1f} s"
 
 
+def cpu_views_sample(pyoracle, views, w, budget_s=4.0):
+    """The oracle on a few rays of the uneven-view batch (each view's own
+    camera, step size and field).  Like the reference it tests every face on
+    every step (no BVH), which on the 82k-triangle scene limits the sample
+    to a few rays per core; returns ray-steps/s, threads and the sample."""
+    threads = pyoracle.max_threads()
+    rng = np.random.default_rng(1)
+    done, steps, rays, t_start = 0, 0, 0, time.perf_counter()
+    order = rng.permutation(len(views))
+    while time.perf_counter() - t_start < budget_s and done < len(order):
+        W, H, camera, params, fidx = views[int(order[done])]
+        pix = np.sort(rng.choice(W * H, size=threads, replace=False)).astype(np.int32)
+        r = pyoracle.render(w.xyz, w.faces, w.face_rgb, camera, w.settings, params, w.fields[fidx], W, H,
+                            pixels=pix, threads=threads, want=("steps",))
+        steps += int(r["steps"].sum())
+        rays += len(pix)
+        done += 1
+    dt = time.perf_counter() - t_start
+    return steps / dt, threads, f"{rays} rays ({threads} per view) of {done} views, brute-force faces, {dt:.1f} s"
+
+
+def bench_configs(eng, wl, predefined_source, pyoracle, cpu):
+    """The other workloads' GPU and CPU numbers: the 512^2 twist frame (h
+    0.01 x 1000 steps), and the oracle on bounded samples of it, of the
+    1024^2 Lyapunov render and of the 64 uneven views."""
+    import torch
+    out = {}
+    w = wl.plain_small()
+    eng.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    fld = eng.compile_field(predefined_source(w.fields[0]))
+    from linon_gb300 import FramePlanes
+    planes = FramePlanes.allocate(w.width, w.height)
+    ts = []
+    with torch.cuda.stream(eng.stream):
+        for i in range(6):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(eng.stream)
+            eng.render(fld, w.camera, w.settings, w.params, planes)
+            b.record(eng.stream)
+            b.synchronize()
+            if i:
+                ts.append(a.elapsed_time(b))
+    steps = int(planes.steps.sum().item())
+    ms = statistics.median(ts)
+    out["plain_512_twist"] = {"workload": w.name, "frame_ms": ms, "ray_steps_per_s": steps / (ms * 1e-3)}
+    if cpu:
+        v, th, smp = cpu_baseline(pyoracle, w, budget_s=3.0)
+        out["plain_512_twist"]["cpu"] = {"value": v, "unit": UNIT, "cores": th, "kind": "port", "sample": smp}
+        w2 = wl.lyapunov_1024()
+        v, th, smp = cpu_baseline(pyoracle, w2, budget_s=3.0)
+        out["lyapunov_1024_render_cpu"] = {"value": v, "unit": UNIT, "cores": th, "kind": "port", "sample": smp}
+        w3 = wl.batch_uneven(64)
+        v, th, smp = cpu_views_sample(pyoracle, w3.extra["views"], w3)
+        out["batch_uneven_64_cpu"] = {"value": v, "unit": UNIT, "cores": th, "kind": "port", "sample": smp}
+    return out
+
+
 def run_reference(args):
     """--impl reference: the reference path's CPU implementation on the host
     cores.  The reference is WGSL run through wgpu on a graphics API, which
@@ -332,6 +389,9 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu:
         v, threads, sample = cpu_baseline(pyoracle, w)
         result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+    # ---- the other workloads: 512^2 twist frame; CPU samples of the rest ----
+    if rank == 0 and world == 1 and not args.no_batch:
+        result["configs"] = bench_configs(eng, wl, predefined_source, pyoracle, cpu=not args.no_cpu)
     if rank == 0:
         print(json.dumps(result))
     eng.close()
