@@ -63,11 +63,14 @@ WG_HD unsigned to_u32(unsigned x) { return x; }
 
 // Sine and cosine of one argument with one range reduction (fast modules).
 // Method: Cody & Waite's additive reduction x = k * P + r, the period split
-// into three floats (pi/2 = P1 + P2 + P3, each product applied by an FMA).
-// Default: P = 2 pi (the split scaled by 4, exact) and sin(r), cos(r) from
+// into floats, each product applied by an FMA.
+// Default: P = 2 pi = P1 + P2 + e (|e| < 7.1e-15) and sin(r), cos(r) from
 // the special-function unit, whose documented absolute error on [-pi, pi]
-// is 2^-21.41; the reduced argument is within 1.3e-7 of the exact
-// x - k * 2 pi for |x| < 2^22.  Measured against FP64: < 5e-7 for
+// is 2^-21.41.  For pi <= |x| < 2^22, x and k * P1 are multiples of 2^-22
+// and differ by less than 4, so x - k * P1 is exact; the one rounding of
+// the P2 step and k * |e| < 4.7e-9 leave the reduced argument within
+// 1.3e-7 of the exact x - k * 2 pi (a third term of the split would change
+// it by no more than k * |e|).  Measured against FP64: < 5e-7 for
 // |x| <= 3000, < 1e-6 for |x| < 2^22 (there the rounding of x / (2 pi) can
 // leave |r| a little above pi); beyond, the error grows with |x|, like the
 // special-function unit's own; inf and NaN give NaN.  No quadrant
@@ -79,9 +82,8 @@ WG_HD void sincos_fast(float x, float* s, float* c) {
 #if defined(__CUDA_ARCH__)
 #if !defined(LINON_SINCOS_POLY)
   const float k = rintf(x * 0x1.45f306p-3f);  // x / (2 pi)
-  float r = fmaf(-k, 0x1.921fb6p+2f, x);      // 2 pi = 4 (P1 + P2 + P3)
+  float r = fmaf(-k, 0x1.921fb6p+2f, x);      // 2 pi = P1 + P2 + e
   r = fmaf(-k, -0x1.777a5cp-23f, r);
-  r = fmaf(-k, -0x1.ee59dap-48f, r);
   *s = __sinf(r);
   *c = __cosf(r);
 #else
