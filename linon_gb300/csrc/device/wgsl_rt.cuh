@@ -236,16 +236,27 @@ struct arr {
   WG_HD const T& operator[](unsigned i) const { return v[i >= unsigned(N) ? unsigned(N - 1) : i]; }
 };
 
+// s * x^-k; for k = 1.5 as (s r)(r r), r = rsqrt(x): two dependent
+// multiplies after the square root instead of three
+WG_HD float scaled_pow_neg_k(float s, float x, float k) {
+#if !defined(LINON_PRECISE) && defined(__CUDA_ARCH__)
+  if (k == 1.5f) {
+    const float r = rsqrtf(x);
+    return (s * r) * (r * r);
+  }
+#endif
+  return s * pow_k(x, -k);
+}
 template <class V> WG_HD V div_pow_k_sv(float s, const V& v, float x, float k) {
 #if !defined(LINON_PRECISE) && defined(__CUDA_ARCH__)
-  return v * (s * pow_k(x, -k));
+  return v * scaled_pow_neg_k(s, x, k);
 #else
   return (s * v) / powf(x, k);
 #endif
 }
 template <class V> WG_HD V div_pow_k_vs(const V& v, float s, float x, float k) {
 #if !defined(LINON_PRECISE) && defined(__CUDA_ARCH__)
-  return v * (s * pow_k(x, -k));
+  return v * scaled_pow_neg_k(s, x, k);
 #else
   return (v * s) / powf(x, k);
 #endif
@@ -573,6 +584,18 @@ WG_HD float dot(const vec2f& a, const vec2f& b) { return a.x * b.x + a.y * b.y; 
 WG_HD float dot(const vec3f& a, const vec3f& b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
 WG_HD float dot(const vec4f& a, const vec4f& b) {
   return ((a.x * b.x + a.y * b.y) + a.z * b.z) + a.w * b.w;
+}
+// dot(a, b) + s (emitted by the front end): precise modules and the host
+// add as written; fast modules start the fused multiply-add chain at s
+// (one operation and one dependent step fewer)
+template <int N> WG_HD float dot_add(const vec<float, N>& a, const vec<float, N>& b, float s) {
+#if defined(LINON_PRECISE) || !defined(__CUDA_ARCH__)
+  return dot(a, b) + s;
+#else
+  float r = fmaf(a.x, b.x, s);
+  for (int i = 1; i < N; ++i) r = fmaf(a[i], b[i], r);
+  return r;
+#endif
 }
 WG_HD int dot(const vec2i& a, const vec2i& b) { return a.x * b.x + a.y * b.y; }
 WG_HD int dot(const vec3i& a, const vec3i& b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }

@@ -2001,6 +2001,20 @@ class Compiler {
         const std::string& op = e.op;
         bool vec = e.args[0]->ty.cat == Ty::Vec || e.args[1]->ty.cat == Ty::Vec;
         if (op == "%" && is_float(e.ty.s)) return "::wgsl::fmod_wgsl(" + a + ", " + b + ")";
+        // dot(a, b) + s or s + dot(a, b) in f32: fast modules fold s into the
+        // dot product's first FMA (wgsl_rt.cuh dot_add); precise modules and
+        // the host add as written (IEEE addition commutes, so either order is
+        // the shader's value)
+        if (op == "+" && e.ty.cat == Ty::Scalar && e.ty.s == SK::F32) {
+          for (int side = 0; side < 2; ++side) {
+            Expr& D = *e.args[size_t(side)];
+            auto ci = callinfo.find(&D);
+            if (D.kind == Expr::Call && !D.cst && ci != callinfo.end() && ci->second.fn == "::wgsl::dot" &&
+                ci->second.targets[0].s == SK::F32)
+              return "::wgsl::dot_add(" + ex_as(*D.args[0], ci->second.targets[0]) + ", " +
+                     ex_as(*D.args[1], ci->second.targets[1]) + ", " + (side == 0 ? b : a) + ")";
+          }
+        }
         // a / pow(x, k) with a constant exponent: fast modules multiply by
         // pow(x, -k) (see wgsl_rt.cuh div_pow_k); precise modules divide
         if (op == "/" && is_float(e.ty.s)) {

@@ -128,6 +128,22 @@ fn bend(v: vec3<f32>, a: f32) -> vec3<f32> {
     assert "u_bend" in code and "field_function" in code
 
 
+def test_dot_plus_scalar_lowering():
+    """dot(a, b) + s in f32, in either order, is emitted as dot_add (fast
+    modules fold s into the first FMA; precise modules add as written);
+    integer dots, vector sums and user functions named like builtins are
+    left alone."""
+    code = translate_wgsl("let a = dot(p, p) + 0.01;\nlet b = 2.0 + dot(v, p);\n"
+                          "let c = dot(vec2<i32>(1, 2), vec2<i32>(3, 4)) + 1;\n"
+                          "return vec3<f32>(a, b, f32(c)) + dot(p, v);")
+    assert code.count("::wgsl::dot_add(") == 2
+    assert "dot_add(u_p, u_p, 0x1.47ae14p-7f)" in code
+    assert "dot_add(u_v, u_p, 2.0f)" in code or "dot_add(u_v, u_p, 0x1p+1f)" in code
+    code = translate_wgsl("return vec3<f32>(mydot(p, p) + 1.0);",
+                          "fn mydot(a: vec3<f32>, b: vec3<f32>) -> f32 { return a.x * b.x; }")
+    assert "dot_add" not in code
+
+
 def test_shadowing_and_abstract_constants():
     code = translate_wgsl("let x = 8.0 / 3.0;\n{ let x = x * 2.0; }\nreturn vec3<f32>(x);")
     # 8/3 folded in double then rounded once to f32
