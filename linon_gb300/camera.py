@@ -136,6 +136,10 @@ class Arcball:
         self.center_translation = _translation(motion[:3]) @ self.center_translation
         self._update()
 
+    def update_screen(self, width: float, height: float):
+        """The window was resized (src/arcball.rs update_screen)."""
+        self.inv_screen = [np.float32(1.0) / np.float32(width), np.float32(1.0) / np.float32(height)]
+
     def uniform(self) -> _abi.Camera:
         """CameraUniform::moving (src/main_view.rs:21-31)."""
         return make_camera(self.eye_pos(), self.eye_dir(), self.up_dir())

@@ -65,6 +65,58 @@ def test_arcball_default_matches_reference_construction():
     assert abs(np.linalg.norm(a.eye_pos() - center) - 2.0) < 1e-4
 
 
+def _angle(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.arccos(np.clip(np.dot(a, b) / np.linalg.norm(a) / np.linalg.norm(b), -1.0, 1.0)))
+
+
+def test_arcball_rotate_is_twice_the_ball_angle():
+    """Shoemake's arcball (src/arcball.rs rotate): dragging from the ball
+    point p to q turns the camera by twice the angle between p and q about
+    p x q; a drag that starts and ends at the same point changes nothing."""
+    center = np.array([0.5, -0.25, 0.1], np.float32)
+    a = cam.Arcball(center, 1.0, (400, 300))
+    eye0, dir0, up0 = a.eye_pos(), a.eye_dir(), a.up_dir()
+    a.rotate((123, 77), (123, 77))
+    np.testing.assert_allclose(a.eye_pos(), eye0, atol=1e-6)
+    np.testing.assert_allclose(a.up_dir(), up0, atol=1e-6)
+    # horizontal drag through the middle row: ball points (0, 0, 1) and
+    # (x, 0, sqrt(1 - x^2)), angle asin(x); the eye turns about the y axis
+    x = 0.3
+    a.rotate((200, 150), (200 + x * 200, 150))
+    np.testing.assert_allclose(_angle(a.eye_dir(), dir0), 2 * np.arcsin(x), atol=2e-6)
+    np.testing.assert_allclose(a.up_dir(), up0, atol=1e-6)
+    assert abs(np.linalg.norm(a.eye_pos() - center) - 1.0) < 1e-5
+    assert abs(a.eye_pos()[1] - eye0[1]) < 1e-6
+    # a drag from the centre to the right edge ends on the ball's rim
+    # (1, 0, 0): a quarter turn between the ball points, a half turn of
+    # the camera
+    b = cam.Arcball(center, 1.0, (400, 300))
+    b.rotate((200, 150), (400, 150))
+    np.testing.assert_allclose(_angle(b.eye_dir(), dir0), np.pi, atol=1e-5)
+
+
+def test_arcball_zoom_pan_and_resize():
+    center = np.array([0.0, 0.0, 0.0], np.float32)
+    a = cam.Arcball(center, 2.0, (640, 480))
+    a.zoom(0.25, 0.5)  # towards the centre by amount * speed * elapsed
+    np.testing.assert_allclose(a.eye_pos(), [0, 0, 0.75], atol=1e-6)
+    # pan scales the pixel delta by |translation[3][3]|, which is 1 for a
+    # translation matrix (the reference reads the w of the translation
+    # column), so a full-width drag moves the view by one unit whatever the
+    # zoom; the eye moves against the drag
+    a.pan((64, 0))
+    np.testing.assert_allclose(a.eye_pos(), [-0.1, 0, 0.75], atol=1e-6)
+    np.testing.assert_allclose(a.eye_dir(), [0, 0, -1], atol=1e-6)
+    a.pan((0, -48))
+    np.testing.assert_allclose(a.eye_pos(), [-0.1, -0.1, 0.75], atol=1e-6)
+    a.update_screen(320, 240)
+    a.pan((32, 0))
+    np.testing.assert_allclose(a.eye_pos(), [-0.2, -0.1, 0.75], atol=1e-6)
+    u = a.uniform()
+    np.testing.assert_allclose(list(u.origin)[:3], a.eye_pos(), atol=1e-7)
+
+
 def test_batch_views_seeded():
     v1 = wl.batch_views(64, seed=0)
     v2 = wl.batch_views(64, seed=0)
