@@ -135,8 +135,10 @@ enum linon_predefined {
 
 /* linon_field_compile flags */
 enum linon_compile_flags {
-  LINON_COMPILE_PRECISE = 1  /* no FMA contraction, IEEE div/sqrt everywhere:
-                                op-for-op the FP32 restatement of the shader */
+  LINON_COMPILE_PRECISE = 1,  /* no FMA contraction, IEEE div/sqrt everywhere:
+                                 op-for-op the FP32 restatement of the shader */
+  LINON_VALIDATE_BATCHED = 2  /* linon_field_validate only: also compile the
+                                 batched kernels (linon_render_batch) with it */
 };
 
 typedef struct linon_ctx linon_ctx;

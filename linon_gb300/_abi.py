@@ -24,6 +24,7 @@ LINON_ESTATE = 8
 LINON_EIO = 9
 LINON_OBJ_NORMALIZE = 1
 LINON_COMPILE_PRECISE = 1
+LINON_VALIDATE_BATCHED = 2
 LINON_MAX_BATCH_FIELDS = 8
 
 FIELD_IDS = {

@@ -581,6 +581,14 @@ int linon_field_validate(const char* field_body, const char* helpers_src, int fl
   // the reference's variant (t-loop, adaptive) and the fixed-step Kahan
   // variant, each with and without the field_weight == 1 specialisation
   int st = jit_check(module_source(t.code, {1, 9, 6, 14}, true), precise, jlog, &bytes);
+  if (st == LINON_OK && (flags & LINON_VALIDATE_BATCHED)) {
+    // the batched kernels (persistent and one CTA per tile) with this field
+    linon_field tmp;
+    tmp.cuda = t.code;
+    std::string blog;
+    st = jit_check(batched_module_source({&tmp}), precise, blog, &bytes);
+    jlog += blog;
+  }
   copy_log(jlog, log, log_cap);
   if (st != LINON_OK) return set_error(st, jlog);
   return LINON_OK;

@@ -171,6 +171,12 @@ int validate_batch(const linon_ctx* ctx, const linon_field* const* fields, int32
 
 }  // namespace
 
+// The batched module (persistent and one-CTA-per-tile kernels) for a list of
+// fields, for compile checks without a context.
+std::string batched_module_source(const std::vector<const linon_field*>& fields) {
+  return batch_module_source(fields);
+}
+
 int batch_tuning(const linon_ctx* ctx, const linon_batch_tuning* in, linon_batch_tuning& t) {
   t = linon_batch_tuning{};
   if (in) t = *in;

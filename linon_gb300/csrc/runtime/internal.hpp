@@ -65,6 +65,7 @@ int jit_compile(const std::string& source, bool precise, const std::vector<std::
 // Compiles `source` to a cubin without loading it (no device needed); the
 // log carries the compiler's and ptxas' messages (registers, spills).
 int jit_check(const std::string& source, bool precise, std::string& log, size_t* cubin_bytes);
+std::string batched_module_source(const std::vector<const linon_field*>& fields);
 
 // ---- BVH ----------------------------------------------------------------
 struct BvhBuild {

@@ -269,11 +269,12 @@ def predefined_name(fid: int) -> str:
     return load().linon_predefined_name(int(fid)).decode()
 
 
-def validate_field(body: str, helpers: str | None = None, precise: bool = False) -> str:
-    """Front end + NVRTC compile without a GPU; returns the compiler report."""
+def validate_field(body: str, helpers: str | None = None, precise: bool = False, batched: bool = False) -> str:
+    """Front end + NVRTC compile without a GPU; returns the compiler report.
+    batched: also compile the batched kernels (linon_render_batch) with it."""
     log = C.create_string_buffer(1 << 18)
-    st = load().linon_field_validate(body.encode(), helpers.encode() if helpers else None,
-                                     _abi.LINON_COMPILE_PRECISE if precise else 0, log, len(log))
+    flags = (_abi.LINON_COMPILE_PRECISE if precise else 0) | (_abi.LINON_VALIDATE_BATCHED if batched else 0)
+    st = load().linon_field_validate(body.encode(), helpers.encode() if helpers else None, flags, log, len(log))
     if st != _abi.LINON_OK:
         raise _abi.LinonCompileError(st, log.value.decode(errors="replace"))
     return log.value.decode(errors="replace")

@@ -28,6 +28,21 @@ def test_every_declared_symbol_is_exported(lib):
     assert set(names) == set(_abi.PROTOTYPES), set(names) ^ set(_abi.PROTOTYPES)
 
 
+def test_constants_match_header():
+    """Every LINON_* enum value and #define the Python bindings restate has
+    the header's value."""
+    text = HEADER.read_text()
+    vals = {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(LINON_[A-Z0-9_]+)\s*=\s*(-?\d+)", text)}
+    vals.update({m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+(LINON_[A-Z0-9_]+)\s+(\d+)", text)})
+    checked = 0
+    for name, v in vals.items():
+        if hasattr(_abi, name):
+            assert getattr(_abi, name) == v, name
+            checked += 1
+    assert checked >= 12
+    assert vals["LINON_VALIDATE_BATCHED"] == _abi.LINON_VALIDATE_BATCHED == 2
+
+
 def test_struct_layouts():
     assert C.sizeof(_abi.Camera) == 112       # CameraUniform, main_view.rs:12-19
     assert C.sizeof(_abi.Settings) == 24      # Settings, main_view.rs:43-51

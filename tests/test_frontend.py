@@ -6,6 +6,7 @@ functions: without FMA contraction both are the same IEEE operations in the
 same order, so every predefined field must agree bit for bit.
 """
 import ctypes as C
+import re
 import subprocess
 import tempfile
 from pathlib import Path
@@ -180,6 +181,15 @@ def test_nvrtc_compiles_for_sm103a(fid, precise):
     report = validate_field(predefined_source(fid), precise=precise)
     assert "linon_march_v14" in report and "linon_march_v1" in report
     assert "sm_103a" in report
+
+
+@pytest.mark.parametrize("name,precise", [("lens", False), ("twist", True)])
+def test_nvrtc_compiles_batched_kernels(name, precise):
+    """LINON_VALIDATE_BATCHED: the batched module (persistent queue and one
+    CTA per tile, each with its three step modes) compiles with the field."""
+    report = validate_field(predefined_source(_abi.FIELD_IDS[name]), precise=precise, batched=True)
+    for k in ("linon_multi_fk", "linon_multi_f", "linon_multi", "linon_batch_fk", "linon_batch_f", "linon_batch"):
+        assert re.search(rf"Function properties for {k}\b", report), k
 
 
 def test_validate_rejects_front_end_errors():
