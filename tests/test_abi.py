@@ -41,6 +41,10 @@ def test_constants_match_header():
             checked += 1
     assert checked >= 12
     assert vals["LINON_VALIDATE_BATCHED"] == _abi.LINON_VALIDATE_BATCHED == 2
+    fields = {k[len("LINON_FIELD_"):].lower(): v for k, v in vals.items()
+              if k.startswith("LINON_FIELD_") and k != "LINON_FIELD_COUNT"}
+    assert fields == _abi.FIELD_IDS
+    assert vals["LINON_FIELD_COUNT"] == _abi.FIELD_COUNT
 
 
 def test_struct_layouts():
