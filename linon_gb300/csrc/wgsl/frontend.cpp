@@ -382,6 +382,7 @@ struct Func {
 struct GConst {
   std::string name;
   int line = 0, col = 0;
+  bool is_override = false;  // `override`: the default value, a concrete scalar
   bool has_ty = false;
   Ty ty;
   EP e;
@@ -408,6 +409,17 @@ class Parser {
         g_structs->push_back(d);
       }
     }
+    // type aliases too (alias Name = Type;), resolved where they are used
+    for (size_t i = 0; i + 3 < t_.size(); ++i) {
+      if (t_[i].t == TT::Ident && t_[i].s == "alias" && t_[i + 1].t == TT::Ident && t_[i + 2].t == TT::Punct &&
+          t_[i + 2].s == "=") {
+        const Tok& nt = t_[i + 1];
+        Ty dummy;
+        if (aliases_.count(nt.s) || struct_id(nt.s) >= 0 || alias_type(nt.s, dummy) || builtin_type_name(nt.s))
+          fail(nt.line, nt.col, "redefinition of type '" + nt.s + "'");
+        aliases_[nt.s] = i + 3;
+      }
+    }
     while (!at_end()) {
       skip_attributes();
       if (is_kw("struct")) {
@@ -415,18 +427,27 @@ class Parser {
       } else if (is_kw("fn")) {
         fns.push_back(function());
       } else if (is_kw("const") || is_kw("let") || is_kw("override")) {
-        if (is_kw("override")) fail(cur().line, cur().col, "override declarations are not supported");
+        const bool ovr = is_kw("override");
         Tok k = next();
         auto g = std::make_unique<GConst>();
         g->line = k.line;
         g->col = k.col;
+        g->is_override = ovr;
         g->name = ident("constant name");
         if (accept(":")) { g->has_ty = true; g->ty = type(); }
+        if (ovr && !is_p("="))
+          fail(k.line, k.col, "override '" + g->name + "' needs a default value: the engine sets no pipeline constants");
         expect("=");
         g->e = expr();
         expect(";");
         consts.push_back(std::move(g));
-      } else if (is_kw("var") || is_kw("alias") || is_kw("enable")) {
+      } else if (is_kw("alias")) {
+        next();
+        ident("alias name");
+        expect("=");
+        type();  // checked here; uses re-read it from aliases_
+        expect(";");
+      } else if (is_kw("var") || is_kw("enable")) {
         fail(cur().line, cur().col, "'" + cur().s + "' declarations are not supported in field function modules");
       } else if (cur().t == TT::Punct && cur().s == ";") {
         next();
@@ -439,6 +460,12 @@ class Parser {
  private:
   std::vector<Tok> t_;
   size_t p_ = 0;
+  std::map<std::string, size_t> aliases_;  // alias name -> first token of its type
+  std::set<std::string> resolving_;         // aliases being resolved (cycle check)
+
+  static bool builtin_type_name(const std::string& n) {
+    return n == "f32" || n == "i32" || n == "u32" || n == "bool" || n == "f16" || n == "f64" || type_generator(n);
+  }
 
   const Tok& cur() const { return t_[p_]; }
   // Closes a template list: '>' or the first '>' of '>>' / '>=' / '>>='
@@ -526,6 +553,17 @@ class Parser {
     if (n == "f16" || n == "f64") fail(k.line, k.col, "type '" + n + "' is not supported");
     Ty t;
     if (alias_type(n, t)) return t;
+    auto ua = aliases_.find(n);
+    if (ua != aliases_.end()) {
+      if (resolving_.count(n)) fail(k.line, k.col, "cyclic type alias '" + n + "'");
+      resolving_.insert(n);
+      const size_t saved = p_;
+      p_ = ua->second;
+      t = type();
+      p_ = saved;
+      resolving_.erase(n);
+      return t;
+    }
     if (struct_id(n) >= 0) {
       t.cat = Ty::Struct;
       t.sid = struct_id(n);
@@ -978,6 +1016,22 @@ class Parser {
         e->has_targ = true;
         e->targ = t;
         if (!is_p("(")) fail(cur().line, cur().col, "expected '(' after type in constructor");
+      } else if (aliases_.count(name) && is_p("(")) {
+        // a type alias used as a constructor: the aliased type's constructor
+        p_--;
+        Ty t = type();
+        e = mkE(Expr::Call, at);
+        if (t.cat == Ty::Struct) {
+          e->op = (*g_structs)[size_t(t.sid)].name;
+        } else if (t.cat == Ty::Scalar) {
+          e->op = wgsl_name(t);
+        } else {
+          e->op = t.cat == Ty::Vec   ? "vec" + std::to_string(t.n)
+                  : t.cat == Ty::Mat ? "mat" + std::to_string(t.n) + "x" + std::to_string(t.r)
+                                     : std::string("array");
+          e->has_targ = true;
+          e->targ = t;
+        }
       } else if (is_p("(")) {
         e = mkE(Expr::Call, at);
         e->op = name;
@@ -1106,6 +1160,16 @@ class Compiler {
     scopes.clear();
     scopes.emplace_back();
     check(*g.e);
+    if (g.is_override) {
+      // an override is a concrete scalar: its declared type, or its default
+      // value's type made concrete
+      if (!g.has_ty) {
+        g.has_ty = true;
+        g.ty = concretize(g.e->ty);
+      }
+      if (g.ty.cat != Ty::Scalar)
+        fail(g.line, g.col, "override '" + g.name + "' must have a scalar type, found " + wgsl_name(g.ty));
+    }
     if (g.has_ty && !(ty_convertible(g.e->ty, g.ty) || g.e->ty == g.ty))
       fail(g.line, g.col, "cannot initialize '" + g.name + "' of type " + wgsl_name(g.ty) + " with " + wgsl_name(g.e->ty));
     Sym s;

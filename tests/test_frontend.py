@@ -447,3 +447,75 @@ def test_struct_diagnostics(helpers, body, needle):
     with pytest.raises(_abi.LinonCompileError) as e:
         translate_wgsl(body, helpers)
     assert needle in e.value.message, e.value.message
+
+
+ALIAS_OVERRIDE_HELPERS = """
+alias Vec = vec3<f32>;
+alias Bend = Ray;               // used before the struct it names
+alias Coeffs = array<Scalar, 3>;
+alias Scalar = f32;             // used (by Coeffs) before its own declaration
+struct Ray { o: Vec, d: Vec }
+@id(0) override strength: f32 = 0.5;
+override steps = 3;             // concrete i32 from an abstract int
+override twice_strength = strength * 2.0;
+fn bend(r: Bend, k: Coeffs) -> Vec {
+    var acc: Vec = r.o;
+    for (var i = 0; i < steps; i++) { acc = acc + k[i] * r.d; }
+    return acc;
+}
+"""
+
+ALIAS_OVERRIDE_BODY = """
+let c = Coeffs(strength, twice_strength, 1.0);
+return bend(Bend(p, v), c);
+"""
+
+
+def test_alias_and_override_semantics():
+    """`alias` names a type (also before its declaration, also a struct);
+    `override` is a pipeline constant whose default value is used (the
+    engine sets no pipeline constants): a concrete scalar, from an abstract
+    initialiser too."""
+    rng = np.random.default_rng(4)
+    x = rng.uniform(-2, 2, (12, 13)).astype(np.float32)
+    out = _host_eval(ALIAS_OVERRIDE_BODY, x, ALIAS_OVERRIDE_HELPERS)
+    p, v = x[:, 3:6], x[:, 9:12]
+    acc = p.copy()
+    for k in (np.float32(0.5), np.float32(1.0), np.float32(1.0)):
+        acc = (acc + k * v).astype(np.float32)
+    np.testing.assert_array_equal(out, acc)
+    assert "linon_march_v1" in validate_field(ALIAS_OVERRIDE_BODY, ALIAS_OVERRIDE_HELPERS)
+
+
+@pytest.mark.parametrize("helpers,needle", [
+    ("alias A = B;\nalias B = A;\nfn f(x: A) -> f32 { return 1.0; }", "cyclic type alias"),
+    ("alias vec3f = vec3<f32>;", "redefinition of type"),
+    ("struct S { a: f32 }\nalias S = f32;", "redefinition of type"),
+    ("alias A = f32;\nalias A = i32;", "redefinition of type"),
+    ("alias A = Nope;\nfn f(x: A) -> f32 { return 1.0; }", "unknown type 'Nope'"),
+    ("override k: f32;", "needs a default value"),
+    ("override k = vec3<f32>(1.0);", "must have a scalar type"),
+    ("override k: i32 = 1.5;", "cannot initialize"),
+])
+def test_alias_override_diagnostics(helpers, needle):
+    with pytest.raises(_abi.LinonCompileError) as e:
+        translate_wgsl("return p;", helpers)
+    assert needle in e.value.message, e.value.message
+
+
+def test_alias_constructors_of_every_kind():
+    """An alias of a vector, matrix or scalar type constructs (and converts)
+    like the type it names."""
+    helpers = "alias V2 = vec2<f32>;\nalias M = mat2x3<f32>;\nalias S = f32;\nalias I = i32;"
+    body = """
+let m = M(V2(1.0, 2.0).xyx, vec3<f32>(p.x, p.y, p.z));
+let s = S(I(2.75));
+return m * V2(t, s) + vec3<f32>(S(3));
+"""
+    rng = np.random.default_rng(8)
+    x = rng.uniform(-2, 2, (6, 13)).astype(np.float32)
+    out = _host_eval(body, x, helpers)
+    p, t = x[:, 3:6], x[:, 12]
+    c0 = np.array([1.0, 2.0, 1.0], np.float32)
+    want = (c0[None, :] * t[:, None] + p * np.float32(2.0) + np.float32(3.0)).astype(np.float32)
+    np.testing.assert_allclose(out, want, rtol=0, atol=1e-6)
