@@ -1,0 +1,45 @@
+"""bench.py's host-side parts, without a GPU: the reference arm's JSON line
+and the CPU samplers behind `cpu_baseline` and `configs`."""
+import json
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[1]
+sys.path.insert(0, str(ROOT))
+
+import bench  # noqa: E402
+from linon_gb300 import workloads as wl  # noqa: E402
+from oracle import pyoracle  # noqa: E402
+
+
+def test_reference_arm_line():
+    """--impl reference prints one JSON line with the contract's keys: the
+    oracle port timed on the host cores, its e2e equal to its value."""
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0",
+                        "--width", "96", "--height", "64"], cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["value"] > 0 and d["unit"] == "ray-steps/s"
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["value"] == d["value"] == d["e2e"]["value"]
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    assert d["config"]["workload"].startswith("cornell_1920x1080")
+
+
+def test_cpu_samplers():
+    w = wl.plain_small(64, 48)
+    v, threads, sample = bench.cpu_baseline(pyoracle, w, budget_s=0.2)
+    assert v > 0 and threads >= 1 and "pixels" in sample
+    views = wl.batch_views(3, seed=2, min_side=16, max_side=24)
+    w.fields = [w.fields[0]] * 3
+    v, threads, sample = bench.cpu_views_sample(pyoracle, views, w, budget_s=0.05)
+    assert v > 0 and "rays" in sample and "views" in sample
+    assert np.isfinite(v)
