@@ -721,6 +721,263 @@ template <int N> WG_HD bool any(const vec<bool, N>& v) {
 }
 
 // ---------------------------------------------------------------------------
+// integer bit builtins (WGSL 17.5: countLeadingZeros ... reverseBits,
+// extractBits, insertBits), component-wise on i32 / u32
+// ---------------------------------------------------------------------------
+WG_HD unsigned clz32_(unsigned x) {
+#if defined(__CUDA_ARCH__)
+  return unsigned(__clz(int(x)));
+#else
+  return x ? unsigned(__builtin_clz(x)) : 32u;
+#endif
+}
+WG_HD unsigned ctz32_(unsigned x) {
+#if defined(__CUDA_ARCH__)
+  return x ? unsigned(__ffs(int(x)) - 1) : 32u;
+#else
+  return x ? unsigned(__builtin_ctz(x)) : 32u;
+#endif
+}
+WG_HD unsigned popc32_(unsigned x) {
+#if defined(__CUDA_ARCH__)
+  return unsigned(__popc(x));
+#else
+  return unsigned(__builtin_popcount(x));
+#endif
+}
+WG_HD unsigned brev32_(unsigned x) {
+#if defined(__CUDA_ARCH__)
+  return __brev(x);
+#else
+  unsigned r = 0;
+  for (int i = 0; i < 32; ++i) r |= ((x >> i) & 1u) << (31 - i);
+  return r;
+#endif
+}
+WG_HD unsigned countLeadingZeros(unsigned x) { return clz32_(x); }
+WG_HD int countLeadingZeros(int x) { return int(clz32_(unsigned(x))); }
+WG_HD unsigned countTrailingZeros(unsigned x) { return ctz32_(x); }
+WG_HD int countTrailingZeros(int x) { return int(ctz32_(unsigned(x))); }
+WG_HD unsigned countOneBits(unsigned x) { return popc32_(x); }
+WG_HD int countOneBits(int x) { return int(popc32_(unsigned(x))); }
+WG_HD unsigned reverseBits(unsigned x) { return brev32_(x); }
+WG_HD int reverseBits(int x) { return int(brev32_(unsigned(x))); }
+// position of the most significant 1 bit (u32), or of the most significant
+// bit that differs from the sign bit (i32); all ones (-1) when there is none
+WG_HD unsigned firstLeadingBit(unsigned x) { return x ? 31u - clz32_(x) : 0xffffffffu; }
+WG_HD int firstLeadingBit(int x) {
+  const unsigned v = x < 0 ? ~unsigned(x) : unsigned(x);
+  return v ? int(31u - clz32_(v)) : -1;
+}
+WG_HD unsigned firstTrailingBit(unsigned x) { return x ? ctz32_(x) : 0xffffffffu; }
+WG_HD int firstTrailingBit(int x) { return x ? int(ctz32_(unsigned(x))) : -1; }
+// bits [o, o + c) with o = min(offset, 32), c = min(count, 32 - o); zero-
+// (u32) or sign-extended (i32); 0 when c = 0
+WG_HD unsigned extractBits(unsigned e, unsigned offset, unsigned count) {
+  const unsigned o = offset < 32u ? offset : 32u, c = count < 32u - o ? count : 32u - o;
+  if (c == 0u) return 0u;
+  return (e >> o) & (c == 32u ? 0xffffffffu : ((1u << c) - 1u));
+}
+WG_HD int extractBits(int e, unsigned offset, unsigned count) {
+  const unsigned o = offset < 32u ? offset : 32u, c = count < 32u - o ? count : 32u - o;
+  if (c == 0u) return 0;
+  return int(unsigned(e) << (32u - o - c)) >> (32u - c);
+}
+// e with bits [o, o + c) replaced by the low c bits of newbits
+WG_HD unsigned insertBits(unsigned e, unsigned newbits, unsigned offset, unsigned count) {
+  const unsigned o = offset < 32u ? offset : 32u, c = count < 32u - o ? count : 32u - o;
+  if (c == 0u) return e;
+  const unsigned mask = (c == 32u ? 0xffffffffu : ((1u << c) - 1u)) << o;
+  return (e & ~mask) | ((newbits << o) & mask);
+}
+WG_HD int insertBits(int e, int newbits, unsigned offset, unsigned count) {
+  return int(insertBits(unsigned(e), unsigned(newbits), offset, count));
+}
+#define WG_BITS1(F)                                                                 \
+  template <class T, int N> WG_HD vec<T, N> F(const vec<T, N>& v) {                \
+    vec<T, N> r;                                                                    \
+    for (int i = 0; i < N; ++i) r[i] = F(v[i]);                                     \
+    return r;                                                                       \
+  }
+WG_BITS1(countLeadingZeros)
+WG_BITS1(countTrailingZeros)
+WG_BITS1(countOneBits)
+WG_BITS1(reverseBits)
+WG_BITS1(firstLeadingBit)
+WG_BITS1(firstTrailingBit)
+#undef WG_BITS1
+template <class T, int N> WG_HD vec<T, N> extractBits(const vec<T, N>& v, unsigned o, unsigned c) {
+  vec<T, N> r;
+  for (int i = 0; i < N; ++i) r[i] = extractBits(v[i], o, c);
+  return r;
+}
+template <class T, int N>
+WG_HD vec<T, N> insertBits(const vec<T, N>& v, const vec<T, N>& nb, unsigned o, unsigned c) {
+  vec<T, N> r;
+  for (int i = 0; i < N; ++i) r[i] = insertBits(v[i], nb[i], o, c);
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// float decomposition: ldexp, frexp, modf (result structs with the WGSL
+// member names), quantizeToF16
+// ---------------------------------------------------------------------------
+template <class F, class I> struct frexp_result {
+  F m_fract;
+  I m_exp;
+};
+template <class F> struct modf_result {
+  F m_fract;
+  F m_whole;
+};
+WG_HD float ldexp(float x, int e) { return ldexpf(x, e); }
+template <int N> WG_HD vec<float, N> ldexp(const vec<float, N>& x, const vec<int, N>& e) {
+  vec<float, N> r;
+  for (int i = 0; i < N; ++i) r[i] = ldexpf(x[i], e[i]);
+  return r;
+}
+WG_HD frexp_result<float, int> frexp(float x) {
+  frexp_result<float, int> r;
+  r.m_fract = frexpf(x, &r.m_exp);
+  return r;
+}
+template <int N> WG_HD frexp_result<vec<float, N>, vec<int, N>> frexp(const vec<float, N>& x) {
+  frexp_result<vec<float, N>, vec<int, N>> r;
+  for (int i = 0; i < N; ++i) r.m_fract[i] = frexpf(x[i], &r.m_exp[i]);
+  return r;
+}
+WG_HD modf_result<float> modf(float x) {
+  modf_result<float> r;
+  r.m_fract = modff(x, &r.m_whole);
+  return r;
+}
+template <int N> WG_HD modf_result<vec<float, N>> modf(const vec<float, N>& x) {
+  modf_result<vec<float, N>> r;
+  for (int i = 0; i < N; ++i) r.m_fract[i] = modff(x[i], &r.m_whole[i]);
+  return r;
+}
+// IEEE binary16 bits of x, rounded to nearest even (overflow to infinity;
+// NaN to a quiet NaN)
+WG_HD unsigned f32_to_f16_bits(float x) {
+  const unsigned u = bitcast_<unsigned>(x);
+  const unsigned sign = (u >> 16) & 0x8000u;
+  const unsigned a = u & 0x7fffffffu;
+  if (a >= 0x7f800000u) return sign | (a > 0x7f800000u ? 0x7e00u : 0x7c00u);
+  if (a >= 0x477ff000u) return sign | 0x7c00u;  // >= 65520 rounds to infinity
+  if (a < 0x38800000u) {
+    // below 2^-14: a binary16 subnormal, the value in units of 2^-24
+    if (a < 0x33000000u) return sign;  // below 2^-25 (half the least subnormal)
+    const unsigned m = (a & 0x007fffffu) | 0x00800000u;  // 24-bit significand
+    const unsigned shift = 126u - (a >> 23);             // to units of 2^-24
+    const unsigned q = m >> shift, rem = m & ((1u << shift) - 1u), half = 1u << (shift - 1u);
+    return sign | (q + ((rem > half || (rem == half && (q & 1u))) ? 1u : 0u));
+  }
+  // normal: rebias the exponent (127 -> 15) and round 23 -> 10 bits
+  const unsigned q = (a - 0x38000000u) >> 13, rem = a & 0x1fffu;
+  return sign | (q + ((rem > 0x1000u || (rem == 0x1000u && (q & 1u))) ? 1u : 0u));
+}
+WG_HD float f16_bits_to_f32(unsigned h) {
+  const unsigned sign = (h & 0x8000u) << 16, e = (h >> 10) & 0x1fu, m = h & 0x3ffu;
+  if (e == 0x1fu) return bitcast_<float>(sign | 0x7f800000u | (m << 13));
+  if (e == 0u) {
+    const float v = float(m) * 5.9604644775390625e-8f;  // m * 2^-24, exact
+    return sign ? -v : v;
+  }
+  return bitcast_<float>(sign | ((e + 112u) << 23) | (m << 13));
+}
+WG_HD float quantizeToF16(float x) { return f16_bits_to_f32(f32_to_f16_bits(x)); }
+template <int N> WG_HD vec<float, N> quantizeToF16(const vec<float, N>& v) {
+  vec<float, N> r;
+  for (int i = 0; i < N; ++i) r[i] = quantizeToF16(v[i]);
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// data packing builtins (WGSL 17.9 / 17.10) and packed 8-bit dot products
+// ---------------------------------------------------------------------------
+WG_HD unsigned pack_snorm_(float x, float s, unsigned mask) {
+  const float c = fminf(1.0f, fmaxf(-1.0f, x));
+  return unsigned(int(floorf(0.5f + s * c))) & mask;
+}
+WG_HD unsigned pack_unorm_(float x, float s) {
+  return unsigned(floorf(0.5f + s * fminf(1.0f, fmaxf(0.0f, x))));
+}
+WG_HD unsigned pack4x8snorm(const vec4f& e) {
+  unsigned r = 0;
+  for (int i = 0; i < 4; ++i) r |= pack_snorm_(e[i], 127.0f, 0xffu) << (8 * i);
+  return r;
+}
+WG_HD unsigned pack4x8unorm(const vec4f& e) {
+  unsigned r = 0;
+  for (int i = 0; i < 4; ++i) r |= pack_unorm_(e[i], 255.0f) << (8 * i);
+  return r;
+}
+WG_HD unsigned pack2x16snorm(const vec2f& e) {
+  return pack_snorm_(e.x, 32767.0f, 0xffffu) | (pack_snorm_(e.y, 32767.0f, 0xffffu) << 16);
+}
+WG_HD unsigned pack2x16unorm(const vec2f& e) {
+  return pack_unorm_(e.x, 65535.0f) | (pack_unorm_(e.y, 65535.0f) << 16);
+}
+WG_HD unsigned pack2x16float(const vec2f& e) { return f32_to_f16_bits(e.x) | (f32_to_f16_bits(e.y) << 16); }
+WG_HD vec4f unpack4x8snorm(unsigned e) {
+  vec4f r;
+  for (int i = 0; i < 4; ++i) r[i] = fmaxf(float(int(e << (24 - 8 * i)) >> 24) / 127.0f, -1.0f);
+  return r;
+}
+WG_HD vec4f unpack4x8unorm(unsigned e) {
+  vec4f r;
+  for (int i = 0; i < 4; ++i) r[i] = float((e >> (8 * i)) & 0xffu) / 255.0f;
+  return r;
+}
+WG_HD vec2f unpack2x16snorm(unsigned e) {
+  return vec2f(fmaxf(float(int(e << 16) >> 16) / 32767.0f, -1.0f), fmaxf(float(int(e) >> 16) / 32767.0f, -1.0f));
+}
+WG_HD vec2f unpack2x16unorm(unsigned e) {
+  return vec2f(float(e & 0xffffu) / 65535.0f, float(e >> 16) / 65535.0f);
+}
+WG_HD vec2f unpack2x16float(unsigned e) { return vec2f(f16_bits_to_f32(e & 0xffffu), f16_bits_to_f32(e >> 16)); }
+WG_HD unsigned pack4xI8(const vec4i& e) {
+  unsigned r = 0;
+  for (int i = 0; i < 4; ++i) r |= (unsigned(e[i]) & 0xffu) << (8 * i);
+  return r;
+}
+WG_HD unsigned pack4xU8(const vec4u& e) {
+  unsigned r = 0;
+  for (int i = 0; i < 4; ++i) r |= (e[i] & 0xffu) << (8 * i);
+  return r;
+}
+WG_HD unsigned pack4xI8Clamp(const vec4i& e) {
+  unsigned r = 0;
+  for (int i = 0; i < 4; ++i) r |= (unsigned(imin_(127, imax_(-128, e[i]))) & 0xffu) << (8 * i);
+  return r;
+}
+WG_HD unsigned pack4xU8Clamp(const vec4u& e) {
+  unsigned r = 0;
+  for (int i = 0; i < 4; ++i) r |= umin_(255u, e[i]) << (8 * i);
+  return r;
+}
+WG_HD vec4i unpack4xI8(unsigned e) {
+  vec4i r;
+  for (int i = 0; i < 4; ++i) r[i] = int(e << (24 - 8 * i)) >> 24;
+  return r;
+}
+WG_HD vec4u unpack4xU8(unsigned e) {
+  vec4u r;
+  for (int i = 0; i < 4; ++i) r[i] = (e >> (8 * i)) & 0xffu;
+  return r;
+}
+WG_HD unsigned dot4U8Packed(unsigned a, unsigned b) {
+  unsigned r = 0;
+  for (int i = 0; i < 4; ++i) r += ((a >> (8 * i)) & 0xffu) * ((b >> (8 * i)) & 0xffu);
+  return r;
+}
+WG_HD int dot4I8Packed(unsigned a, unsigned b) {
+  int r = 0;
+  for (int i = 0; i < 4; ++i) r += (int(a << (24 - 8 * i)) >> 24) * (int(b << (24 - 8 * i)) >> 24);
+  return r;
+}
+
+// ---------------------------------------------------------------------------
 // linon helper functions, src/main_view.wgsl:76-146
 // ---------------------------------------------------------------------------
 #define LINON_PI 3.14159265358979323846f

@@ -53,6 +53,7 @@ struct StructDef {
   std::string name;
   int line = 0, col = 0;
   std::vector<std::pair<std::string, Ty>> members;
+  std::string cpp;  // built-in result structs (frexp, modf): the runtime's type
 };
 thread_local std::vector<StructDef>* g_structs = nullptr;
 int struct_id(const std::string& n) {
@@ -130,7 +131,9 @@ std::string cpp_name(const Ty& t) {
     case Ty::Vec: return std::string("::wgsl::vec<") + sk_cpp(t.s) + "," + std::to_string(t.n) + ">";
     case Ty::Mat: return "::wgsl::mat<" + std::to_string(t.n) + "," + std::to_string(t.r) + ">";
     case Ty::Arr: return "::wgsl::arr<" + cpp_name(elemT(t)) + "," + std::to_string(t.alen) + ">";
-    case Ty::Struct: return "s_" + (g_structs && t.sid >= 0 ? (*g_structs)[size_t(t.sid)].name : std::string("?"));
+    case Ty::Struct:
+      if (g_structs && t.sid >= 0 && !(*g_structs)[size_t(t.sid)].cpp.empty()) return (*g_structs)[size_t(t.sid)].cpp;
+      return "s_" + (g_structs && t.sid >= 0 ? (*g_structs)[size_t(t.sid)].name : std::string("?"));
   }
   return "?";
 }
@@ -495,6 +498,8 @@ class Parser {
     static const std::set<std::string> kw = {"fn", "let", "var", "const", "if", "else", "for", "while", "loop",
                                              "return", "break", "continue", "true", "false", "struct", "continuing"};
     if (kw.count(cur().s)) fail(cur().line, cur().col, "'" + cur().s + "' is a reserved keyword");
+    if (cur().s.size() >= 2 && cur().s[0] == '_' && cur().s[1] == '_')
+      fail(cur().line, cur().col, "identifiers starting with '__' are reserved");
     return next().s;
   }
   void skip_attributes() {
@@ -1926,6 +1931,132 @@ class Compiler {
       callinfo[&e] = ci;
       return;
     }
+    // ---- integer bit builtins: i32 / u32 scalars and vectors ----
+    auto int_arg = [&](size_t i) {
+      Expr& a = *e.args[i];
+      if (!((a.ty.cat == Ty::Scalar || a.ty.cat == Ty::Vec) &&
+            (a.ty.s == SK::I32 || a.ty.s == SK::U32 || a.ty.s == SK::AInt)))
+        fail(a.line, a.col, "'" + n + "' needs an i32 or u32 scalar or vector, found " + wgsl_name(a.ty));
+      return concretize(a.ty);
+    };
+    auto fixed_arg = [&](size_t i, const Ty& want) {
+      Expr& a = *e.args[i];
+      if (!(a.ty == want || ty_convertible(a.ty, want)))
+        fail(a.line, a.col, "argument " + std::to_string(i + 1) + " of '" + n + "' must be " + wgsl_name(want) +
+                                ", found " + wgsl_name(a.ty));
+      return want;
+    };
+    auto float_arg = [&](size_t i) {
+      Expr& a = *e.args[i];
+      if (!((a.ty.cat == Ty::Scalar || a.ty.cat == Ty::Vec) &&
+            (a.ty.s == SK::F32 || a.ty.s == SK::AFloat || a.ty.s == SK::AInt)))
+        fail(a.line, a.col, "'" + n + "' needs an f32 scalar or vector, found " + wgsl_name(a.ty));
+      Ty t = a.ty;
+      t.s = SK::F32;
+      return t;
+    };
+    auto finish = [&](const Ty& result, std::vector<Ty> targets, int fl) {
+      e.ty = result;
+      e.fl += fl;
+      ci.targets = std::move(targets);
+      callinfo[&e] = ci;
+    };
+    static const std::set<std::string> bits1 = {"countLeadingZeros", "countOneBits", "countTrailingZeros",
+                                                "reverseBits", "firstLeadingBit", "firstTrailingBit"};
+    if (bits1.count(n)) {
+      need_args(e, 1);
+      const Ty t = int_arg(0);
+      return finish(t, {t}, 0);
+    }
+    if (n == "extractBits") {
+      need_args(e, 3);
+      const Ty t = int_arg(0), u = scalar(SK::U32);
+      return finish(t, {t, fixed_arg(1, u), fixed_arg(2, u)}, 0);
+    }
+    if (n == "insertBits") {
+      need_args(e, 4);
+      const Ty t = int_arg(0), u = scalar(SK::U32);
+      return finish(t, {t, fixed_arg(1, t), fixed_arg(2, u), fixed_arg(3, u)}, 0);
+    }
+    // ---- float decomposition ----
+    if (n == "ldexp") {
+      need_args(e, 2);
+      const Ty t = float_arg(0);
+      Ty ti = t;
+      ti.s = SK::I32;
+      return finish(t, {t, fixed_arg(1, ti)}, vcount(t));
+    }
+    if (n == "quantizeToF16") {
+      need_args(e, 1);
+      const Ty t = float_arg(0);
+      return finish(t, {t}, 0);
+    }
+    if (n == "frexp" || n == "modf") {
+      need_args(e, 1);
+      const Ty t = float_arg(0);
+      Ty ti = t;
+      ti.s = SK::I32;
+      // WGSL's built-in result structure (__frexp_result_f32,
+      // __modf_result_vec3_f32, ...): fract and exp, or fract and whole
+      const std::string shape = t.cat == Ty::Vec ? "vec" + std::to_string(t.n) + "_f32" : std::string("f32");
+      const std::string sname = "__" + n + "_result_" + shape;
+      int sid = struct_id(sname);
+      if (sid < 0) {
+        StructDef d;
+        d.name = sname;
+        if (n == "frexp") {
+          d.members = {{"fract", t}, {"exp", ti}};
+          d.cpp = "::wgsl::frexp_result<" + cpp_name(t) + "," + cpp_name(ti) + ">";
+        } else {
+          d.members = {{"fract", t}, {"whole", t}};
+          d.cpp = "::wgsl::modf_result<" + cpp_name(t) + ">";
+        }
+        g_structs->push_back(d);
+        sid = int(g_structs->size()) - 1;
+      }
+      Ty st;
+      st.cat = Ty::Struct;
+      st.sid = sid;
+      return finish(st, {t}, n == "modf" ? vcount(t) : 0);
+    }
+    // ---- data packing ----
+    const Ty u32t = scalar(SK::U32), v4f = vecT(SK::F32, 4), v2f = vecT(SK::F32, 2);
+    if (n == "pack4x8snorm" || n == "pack4x8unorm") {
+      need_args(e, 1);
+      return finish(u32t, {fixed_arg(0, v4f)}, 12);
+    }
+    if (n == "pack2x16snorm" || n == "pack2x16unorm" || n == "pack2x16float") {
+      need_args(e, 1);
+      return finish(u32t, {fixed_arg(0, v2f)}, n == "pack2x16float" ? 0 : 6);
+    }
+    if (n == "unpack4x8snorm" || n == "unpack4x8unorm") {
+      need_args(e, 1);
+      return finish(v4f, {fixed_arg(0, u32t)}, 4);
+    }
+    if (n == "unpack2x16snorm" || n == "unpack2x16unorm" || n == "unpack2x16float") {
+      need_args(e, 1);
+      return finish(v2f, {fixed_arg(0, u32t)}, n == "unpack2x16float" ? 0 : 2);
+    }
+    if (n == "pack4xI8" || n == "pack4xI8Clamp") {
+      need_args(e, 1);
+      return finish(u32t, {fixed_arg(0, vecT(SK::I32, 4))}, 0);
+    }
+    if (n == "pack4xU8" || n == "pack4xU8Clamp") {
+      need_args(e, 1);
+      return finish(u32t, {fixed_arg(0, vecT(SK::U32, 4))}, 0);
+    }
+    if (n == "unpack4xI8") {
+      need_args(e, 1);
+      return finish(vecT(SK::I32, 4), {fixed_arg(0, u32t)}, 0);
+    }
+    if (n == "unpack4xU8") {
+      need_args(e, 1);
+      return finish(vecT(SK::U32, 4), {fixed_arg(0, u32t)}, 0);
+    }
+    if (n == "dot4U8Packed" || n == "dot4I8Packed") {
+      need_args(e, 2);
+      return finish(scalar(n == "dot4U8Packed" ? SK::U32 : SK::I32), {fixed_arg(0, u32t), fixed_arg(1, u32t)}, 0);
+    }
     if (n == "dot") {
       need_args(e, 2);
       Ty t = concretize(unify_args(e, 0, 2, false, true));
@@ -2588,6 +2719,9 @@ Translation translate(const std::string& field_body, const std::string& helpers_
       order.push_back(i);
     };
     for (size_t i = 0; i < structs.size(); ++i) visit(int(i));
+    // room for the built-in result structs the checker adds (frexp and modf
+    // of f32 and vec2..4), so references into the list stay valid
+    structs.reserve(structs.size() + 8);
     cc.declare_module(0);
     Func* field = nullptr;
     for (auto& f : cc.fns)

@@ -519,3 +519,249 @@ return m * V2(t, s) + vec3<f32>(S(3));
     c0 = np.array([1.0, 2.0, 1.0], np.float32)
     want = (c0[None, :] * t[:, None] + p * np.float32(2.0) + np.float32(3.0)).astype(np.float32)
     np.testing.assert_allclose(out, want, rtol=0, atol=1e-6)
+
+
+# ---- bit, float-decomposition and packing builtins (WGSL 17.5 / 17.9 / 17.10) ----
+M32 = 0xFFFFFFFF
+
+
+def _s32(u):
+    u &= M32
+    return u - (1 << 32) if u & 0x80000000 else u
+
+
+def _clz(u):
+    return 32 - (u & M32).bit_length()
+
+
+def _ctz(u):
+    u &= M32
+    return 32 if u == 0 else (u & -u).bit_length() - 1
+
+
+def _rev(u):
+    return int(f"{u & M32:032b}"[::-1], 2)
+
+
+def _flb_i(i):
+    v = ~i if i < 0 else i
+    return -1 if v == 0 else v.bit_length() - 1
+
+
+def _ext_u(e, off, cnt):
+    o = min(off, 32)
+    c = min(cnt, 32 - o)
+    return 0 if c == 0 else (e >> o) & ((1 << c) - 1)
+
+
+def _ext_i(e, off, cnt):
+    o = min(off, 32)
+    c = min(cnt, 32 - o)
+    if c == 0:
+        return 0
+    v = (e & M32) >> o & ((1 << c) - 1)
+    return v - (1 << c) if v >> (c - 1) else v
+
+
+def _ins(e, nb, off, cnt):
+    o = min(off, 32)
+    c = min(cnt, 32 - o)
+    if c == 0:
+        return e & M32
+    mask = ((1 << c) - 1) << o
+    return ((e & ~mask) | ((nb << o) & mask)) & M32
+
+
+def _bits_inputs(n=3000):
+    rng = np.random.default_rng(21)
+    x = np.zeros((n, 13), np.float32)
+    raw = rng.integers(0, 2 ** 32, (n, 3), dtype=np.uint64).astype(np.uint32)
+    raw[:40] = [[0, 0, 0], [M32, M32, M32], [1, 2, 3], [0x80000000, 0x7FFFFFFF, 0x00010000]] * 10
+    raw[40:80, 2] = rng.integers(0, 70, 40)  # small offsets / counts, including > 32
+    x[:, 3:6] = raw.view(np.float32)
+    x[:, 12] = rng.integers(0, 40, n).astype(np.float32)
+    return x, raw
+
+
+def test_integer_bit_builtins():
+    x, raw = _bits_inputs()
+    body = """
+let u = bitcast<u32>(p.x);
+let i = bitcast<i32>(p.y);
+let w = bitcast<u32>(p.z);
+let o = u32(t);
+let c = w % 40u;
+let a = countLeadingZeros(u) | (countOneBits(u) << 8u) | (countTrailingZeros(u) << 16u)
+      | (u32(countOneBits(i)) << 24u);
+return bitcast<vec3<f32>>(vec3<u32>(a, reverseBits(u), bitcast<u32>(firstLeadingBit(i))));
+"""
+    out = _host_eval(body, x).view(np.uint32)
+    for k in range(len(x)):
+        u, i = int(raw[k, 0]), _s32(int(raw[k, 1]))
+        a = _clz(u) | (bin(u).count("1") << 8) | (_ctz(u) << 16) | (bin(i & M32).count("1") << 24)
+        assert list(out[k]) == [a, _rev(u), _flb_i(i) & M32], k
+    body2 = """
+let u = bitcast<u32>(p.x);
+let i = bitcast<i32>(p.y);
+let w = bitcast<u32>(p.z);
+let o = u32(t);
+let c = w % 40u;
+return bitcast<vec3<f32>>(vec3<u32>(firstTrailingBit(u) ^ (firstLeadingBit(u) << 7u),
+                                    extractBits(u, o, c) ^ bitcast<u32>(extractBits(i, o, c)),
+                                    insertBits(u, w, o, c) ^ bitcast<u32>(insertBits(i, bitcast<i32>(w), c, o))));
+"""
+    out = _host_eval(body2, x).view(np.uint32)
+    for k in range(len(x)):
+        u, i, w = int(raw[k, 0]), _s32(int(raw[k, 1])), int(raw[k, 2])
+        o, c = int(x[k, 12]), w % 40
+        ftb = M32 if u == 0 else _ctz(u)
+        flb = M32 if u == 0 else u.bit_length() - 1
+        e0 = (ftb ^ (flb << 7)) & M32
+        e1 = (_ext_u(u, o, c) ^ (_ext_i(i, o, c) & M32)) & M32
+        e2 = _ins(u, w, o, c) ^ _ins(i & M32, w, c, o)
+        assert list(out[k]) == [e0, e1, e2], k
+    # vectors, component-wise
+    vb = "let u = bitcast<vec3<u32>>(p);\nreturn bitcast<vec3<f32>>(countOneBits(u) + reverseBits(u));"
+    out = _host_eval(vb, x).view(np.uint32)
+    want = [[(bin(int(q)).count("1") + _rev(int(q))) & M32 for q in r] for r in raw]
+    np.testing.assert_array_equal(out, np.array(want, np.uint32))
+
+
+def test_float_decomposition_builtins():
+    rng = np.random.default_rng(22)
+    n = 4000
+    x = np.zeros((n, 13), np.float32)
+    vals = np.concatenate([rng.uniform(-1e6, 1e6, n // 2), rng.standard_normal(n // 4) * 1e-3,
+                           rng.uniform(-70000, 70000, n - n // 2 - n // 4)]).astype(np.float32)
+    vals[:6] = [0.0, -0.0, 1.0, -2.5, 65519.0, 65520.0]
+    x[:, 3] = vals
+    x[:, 4] = rng.uniform(-3, 3, n).astype(np.float32)
+    x[:, 12] = rng.integers(-30, 30, n).astype(np.float32)
+    body = """
+let f = frexp(p.x);
+let m = modf(p.x);
+return vec3<f32>(f.fract + f32(f.exp) * 2.0, m.fract + m.whole * 0.5, ldexp(p.y, i32(t)));
+"""
+    out = _host_eval(body, x)
+    fr, ex = np.frexp(vals)
+    mf, mw = np.modf(vals)
+    want = np.stack([fr.astype(np.float32) + ex.astype(np.float32) * np.float32(2.0),
+                     mf.astype(np.float32) + mw.astype(np.float32) * np.float32(0.5),
+                     np.ldexp(x[:, 4], x[:, 12].astype(np.int32)).astype(np.float32)], -1)
+    np.testing.assert_array_equal(out, want)
+    q = _host_eval("let f = frexp(vec3<f32>(p.x, p.y, 0.0));\n"
+                   "return quantizeToF16(vec3<f32>(p.x, p.y, f32(f.exp.y)));", x)
+    with np.errstate(over="ignore"):
+        np.testing.assert_array_equal(q[:, :2], x[:, 3:5].astype(np.float16).astype(np.float32))
+    np.testing.assert_array_equal(q[:, 2], np.frexp(x[:, 4])[1].astype(np.float16).astype(np.float32))
+
+
+def test_packing_builtins():
+    rng = np.random.default_rng(23)
+    n = 3000
+    x = np.zeros((n, 13), np.float32)
+    x[:, 3:6] = rng.uniform(-1.5, 1.5, (n, 3)).astype(np.float32)
+    x[:, 12] = rng.uniform(-1.5, 1.5, n).astype(np.float32)
+    x[:10, 3:6] = [[1, -1, 0.5], [0.00196, -0.00196, 0.0039], [2, -2, 0]] * 3 + [[1e-8, -1e-8, 65504]]
+    body = """
+let e = vec4<f32>(p, t);
+return bitcast<vec3<f32>>(vec3<u32>(pack4x8snorm(e), pack4x8unorm(e), pack2x16float(p.xy)));
+"""
+    out = _host_eval(body, x).view(np.uint32)
+    e4 = np.concatenate([x[:, 3:6], x[:, 12:13]], 1)
+
+    def pk(vals, s, lo, bits):
+        c = np.minimum(np.float32(1), np.maximum(np.float32(lo), vals))
+        q = np.floor(np.float32(0.5) + np.float32(s) * c).astype(np.int64) & ((1 << bits) - 1)
+        return sum(q[:, j] << (bits * j) for j in range(vals.shape[1]))
+    h = x[:, 3:5].astype(np.float16).view(np.uint16).astype(np.int64)
+    want = np.stack([pk(e4, 127, -1, 8), pk(e4, 255, 0, 8), h[:, 0] | (h[:, 1] << 16)], -1).astype(np.uint32)
+    np.testing.assert_array_equal(out, want)
+    body = """
+let s = pack2x16snorm(p.xy);
+let u = pack2x16unorm(p.yz);
+return vec3<f32>(dot(unpack2x16snorm(s), vec2<f32>(1.0, 1000.0)), dot(unpack2x16unorm(u), vec2<f32>(1.0, 1000.0)),
+                 unpack4x8snorm(pack4x8snorm(vec4<f32>(p, t))).w + 10.0 * unpack4x8unorm(pack4x8unorm(vec4<f32>(p, t))).x);
+"""
+    out = _host_eval(body, x)
+    s16 = pk(x[:, 3:5], 32767, -1, 16)
+    u16 = pk(x[:, 4:6], 65535, 0, 16)
+
+    def sx(v, b):
+        v = v & ((1 << b) - 1)
+        return np.where(v >= 1 << (b - 1), v - (1 << b), v)
+    us0 = np.maximum(sx(s16, 16).astype(np.float32) / np.float32(32767), np.float32(-1))
+    us1 = np.maximum(sx(s16 >> 16, 16).astype(np.float32) / np.float32(32767), np.float32(-1))
+    uu0 = (u16 & 0xFFFF).astype(np.float32) / np.float32(65535)
+    uu1 = (u16 >> 16).astype(np.float32) / np.float32(65535)
+    p8s = pk(e4, 127, -1, 8)
+    p8u = pk(e4, 255, 0, 8)
+    w3 = np.maximum(sx(p8s >> 24, 8).astype(np.float32) / np.float32(127), np.float32(-1))
+    x0 = (p8u & 0xFF).astype(np.float32) / np.float32(255)
+    want = np.stack([us0 + us1 * np.float32(1000), uu0 + uu1 * np.float32(1000), w3 + np.float32(10) * x0], -1)
+    np.testing.assert_array_equal(out, want.astype(np.float32))
+    # unpack2x16float round trip, 8-bit integer packing and packed dot products
+    body = """
+let a = bitcast<u32>(p.x);
+let b = bitcast<u32>(p.y);
+let vi = vec4<i32>(i32(t * 200.0), -3, 130, -200);
+let vu = vec4<u32>(u32(abs(t) * 200.0), 3u, 300u, 255u);
+let r = unpack4xI8(pack4xI8(vi)) + unpack4xI8(pack4xI8Clamp(vi)) * 1000;
+let q = unpack4xU8(pack4xU8(vu)) + unpack4xU8(pack4xU8Clamp(vu)) * 1000u;
+return bitcast<vec3<f32>>(vec3<u32>(dot4U8Packed(a, b), bitcast<u32>(dot4I8Packed(a, b)),
+                                    bitcast<u32>(r.x + r.y + r.z * 7 + r.w * 13) ^ (q.x + q.z * 7u + q.w * 13u)));
+"""
+    x2 = x.copy()
+    x2[:, 3:5] = rng.integers(0, 2 ** 32, (n, 2), dtype=np.uint64).astype(np.uint32).view(np.float32)
+    out = _host_eval(body, x2).view(np.uint32)
+    A = x2[:, 3].view(np.uint32).astype(np.int64)
+    B = x2[:, 4].view(np.uint32).astype(np.int64)
+    du = sum(((A >> (8 * j)) & 0xFF) * ((B >> (8 * j)) & 0xFF) for j in range(4))
+    di = sum(sx(A >> (8 * j), 8) * sx(B >> (8 * j), 8) for j in range(4))
+    t = x2[:, 12]
+    vi = [(t * np.float32(200)).astype(np.int64), np.full(n, -3), np.full(n, 130), np.full(n, -200)]
+    vu = [(np.abs(t) * np.float32(200)).astype(np.int64), np.full(n, 3), np.full(n, 300), np.full(n, 255)]
+    r = [sx(v, 8) + np.clip(v, -128, 127) * 1000 for v in vi]
+    q = [(v & 0xFF) + np.minimum(v, 255) * 1000 for v in vu]
+    e2 = ((r[0] + r[1] + r[2] * 7 + r[3] * 13) & M32) ^ ((q[0] + q[2] * 7 + q[3] * 13) & M32)
+    np.testing.assert_array_equal(out, np.stack([du & M32, di & M32, e2], -1).astype(np.uint32))
+    h2 = _host_eval("return vec3<f32>(unpack2x16float(pack2x16float(p.xy)), 0.0);", x)
+    np.testing.assert_array_equal(h2[:, :2], x[:, 3:5].astype(np.float16).astype(np.float32))
+
+
+@pytest.mark.parametrize("body,needle", [
+    ("let a = countOneBits(1.5); return p;", "needs an i32 or u32"),
+    ("let a = extractBits(1u, 2, 1.5); return p;", "must be u32"),
+    ("let a = extractBits(1u, 2, -1); return p;", "does not fit in u32"),
+    ("let a = ldexp(p, 2); return p;", "must be vec3<i32>"),
+    ("let a = pack4x8snorm(p); return p;", "must be vec4<f32>"),
+    ("let f = frexp(p.x); return vec3<f32>(f.whole);", "has no member 'whole'"),
+    ("let __x = 1.0; return p;", "reserved"),
+])
+def test_builtin_diagnostics(body, needle):
+    with pytest.raises(_abi.LinonCompileError) as e:
+        translate_wgsl(body)
+    assert needle in e.value.message, e.value.message
+
+
+ALL_NEW_BUILTINS_BODY = """
+let u = bitcast<u32>(p.x);
+let i = bitcast<i32>(p.y);
+let a = countLeadingZeros(u) + countOneBits(u) + countTrailingZeros(u) + reverseBits(u) + firstLeadingBit(u)
+      + firstTrailingBit(u) + extractBits(u, 3u, 5u) + insertBits(u, 7u, 2u, 3u);
+let b = countLeadingZeros(vec2<i32>(i)) + firstLeadingBit(vec2<i32>(i)) + extractBits(vec2<i32>(i), 1u, 9u);
+let f = frexp(p);
+let m = modf(p.x);
+let e = vec4<f32>(p, t);
+let k = pack4x8snorm(e) ^ pack4x8unorm(e) ^ pack2x16snorm(p.xy) ^ pack2x16unorm(p.xy) ^ pack2x16float(p.xy)
+      ^ pack4xI8(vec4<i32>(b, b)) ^ pack4xU8(unpack4xU8(u)) ^ pack4xI8Clamp(unpack4xI8(u)) ^ pack4xU8Clamp(vec4<u32>(a));
+let g = unpack4x8snorm(k).xyz + unpack4x8unorm(k).xyz + vec3<f32>(unpack2x16snorm(k) + unpack2x16unorm(k)
+      + unpack2x16float(k), f32(dot4U8Packed(k, u)) + f32(dot4I8Packed(k, u)));
+return g + ldexp(f.fract, f.exp) + quantizeToF16(vec3<f32>(m.fract, m.whole, f32(a)));
+"""
+
+
+@pytest.mark.parametrize("precise", [False, True])
+def test_new_builtins_compile_for_sm103a(precise):
+    report = validate_field(ALL_NEW_BUILTINS_BODY, precise=precise)
+    assert "linon_march_v14" in report and "sm_103a" in report
