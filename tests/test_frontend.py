@@ -765,3 +765,27 @@ return g + ldexp(f.fract, f.exp) + quantizeToF16(vec3<f32>(m.fract, m.whole, f32
 def test_new_builtins_compile_for_sm103a(precise):
     report = validate_field(ALL_NEW_BUILTINS_BODY, precise=precise)
     assert "linon_march_v14" in report and "sm_103a" in report
+
+
+def test_f16_conversions_every_value():
+    """unpack2x16float decodes every binary16 bit pattern exactly, and
+    pack2x16float encodes each decoded value back to its own bits (NaNs to a
+    NaN)."""
+    h = np.arange(65536, dtype=np.uint32)
+    words = (h[0::2] | (h[1::2] << 16)).astype(np.uint32)
+    x = np.zeros((len(words), 13), np.float32)
+    x[:, 3] = words.view(np.float32)
+    out = _host_eval("let w = bitcast<u32>(p.x);\nlet f = unpack2x16float(w);\n"
+                     "return vec3<f32>(f, bitcast<f32>(pack2x16float(f)));", x)
+    ref = h.astype(np.uint16).view(np.float16).astype(np.float32)
+    got = np.stack([out[:, 0], out[:, 1]], 1).reshape(-1)
+    nan = np.isnan(ref)
+    np.testing.assert_array_equal(got[~nan].view(np.uint32), ref[~nan].view(np.uint32))
+    assert np.isnan(got[nan]).all()
+    back = out[:, 2].view(np.uint32)
+    lo, hi = back & 0xFFFF, back >> 16
+    rt = np.stack([lo, hi], 1).reshape(-1)
+    ok = nan | (rt == h)
+    assert ok.all()
+    nh = rt[nan]
+    assert (((nh & 0x7C00) == 0x7C00) & ((nh & 0x3FF) != 0)).all()
