@@ -789,3 +789,48 @@ def test_f16_conversions_every_value():
     assert ok.all()
     nh = rt[nan]
     assert (((nh & 0x7C00) == 0x7C00) & ((nh & 0x3FF) != 0)).all()
+
+
+@pytest.mark.gpu
+def test_new_builtins_device_equals_host(engine):
+    """The device implementations of the bit, decomposition and packing
+    builtins (CUDA integer intrinsics, ldexpf / frexpf / modff) give the
+    host implementations' results bit for bit (precise module, through
+    linon_field_eval)."""
+    import torch
+    bodies = [
+        # integer bits, as u32 bit patterns
+        """let u = bitcast<u32>(p.x);
+let i = bitcast<i32>(p.y);
+let w = bitcast<u32>(p.z);
+let o = u32(t);
+let c = w % 40u;
+return bitcast<vec3<f32>>(vec3<u32>(
+    countLeadingZeros(u) | (countOneBits(u) << 8u) | (countTrailingZeros(u) << 16u),
+    reverseBits(u) ^ bitcast<u32>(firstLeadingBit(i)) ^ firstTrailingBit(u) ^ (firstLeadingBit(u) << 3u),
+    extractBits(u, o, c) ^ bitcast<u32>(extractBits(i, o, c)) ^ insertBits(u, w, o, c)));""",
+        # packing and packed dot products
+        """let u = bitcast<u32>(p.x);
+let w = bitcast<u32>(p.z);
+let e = vec4<f32>(v, t);
+return bitcast<vec3<f32>>(vec3<u32>(pack4x8snorm(e) ^ pack2x16float(v.xy),
+    pack4x8unorm(e) ^ pack2x16snorm(v.yz) ^ pack2x16unorm(v.xz),
+    dot4U8Packed(u, w) ^ bitcast<u32>(dot4I8Packed(u, w)) ^ pack4xI8Clamp(unpack4xI8(u)) ^ pack4xU8(unpack4xU8(w))));""",
+        # unpacking and decomposition, as floats
+        """let u = bitcast<u32>(p.x);
+let f = frexp(v);
+let m = modf(v.x * 100.0);
+return unpack4x8snorm(u).xyz + unpack4x8unorm(u).xyz + vec3<f32>(unpack2x16float(u), 0.0)
+     + f.fract + vec3<f32>(f.exp) * 0.25 + vec3<f32>(m.fract, m.whole, ldexp(v.y, i32(t) - 20))
+     + quantizeToF16(v * 1000.0);""",
+    ]
+    x, _ = _bits_inputs(2048)
+    rng = np.random.default_rng(31)
+    x[:, 9:12] = rng.uniform(-3, 3, (len(x), 3)).astype(np.float32)
+    for body in bodies:
+        fld = engine.compile_field(body, precise=True)
+        dev = engine.field_eval(fld, torch.from_numpy(x).cuda()).cpu().numpy()
+        host = _host_eval(body, x)
+        both_nan = np.isnan(dev) & np.isnan(host)  # NaN payloads differ between CPU and GPU
+        np.testing.assert_array_equal(np.where(both_nan, 0, dev.view(np.uint32)),
+                                      np.where(both_nan, 0, host.view(np.uint32)))
