@@ -827,10 +827,13 @@ return unpack4x8snorm(u).xyz + unpack4x8unorm(u).xyz + vec3<f32>(unpack2x16float
     x, _ = _bits_inputs(2048)
     rng = np.random.default_rng(31)
     x[:, 9:12] = rng.uniform(-3, 3, (len(x), 3)).astype(np.float32)
-    for body in bodies:
+    for k, body in enumerate(bodies):
         fld = engine.compile_field(body, precise=True)
         dev = engine.field_eval(fld, torch.from_numpy(x).cuda()).cpu().numpy()
         host = _host_eval(body, x)
-        both_nan = np.isnan(dev) & np.isnan(host)  # NaN payloads differ between CPU and GPU
+        # the first two return integer bit patterns (compared as they are);
+        # the last computes in floats, whose NaN payloads differ between the
+        # CPU and the GPU
+        both_nan = (np.isnan(dev) & np.isnan(host)) if k == 2 else np.zeros(dev.shape, bool)
         np.testing.assert_array_equal(np.where(both_nan, 0, dev.view(np.uint32)),
                                       np.where(both_nan, 0, host.view(np.uint32)))
