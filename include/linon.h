@@ -441,6 +441,14 @@ int linon_serve_stop(linon_server* server);
  * SM, best of 5 launches timed with CUDA events), in TFLOP/s.             */
 int linon_probe_fp32_peak(linon_ctx* ctx, double* tflops);
 
+/* ---- failure path --------------------------------------------------------
+ * Runs one CTA that waits, with the march kernels' bounded mbarrier wait, on
+ * a barrier that nothing completes (no copy is issued), for at most `polls`
+ * polls (1..2^24): the wait runs out, the kernel sets error bit 1 and
+ * returns, and the call returns what linon_synchronize reports for it:
+ * LINON_ETIMEOUT (error word cleared; the context stays usable).            */
+int linon_check_bounded_wait(linon_ctx* ctx, int32_t polls);
+
 #ifdef __cplusplus
 }
 #endif

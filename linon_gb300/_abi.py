@@ -156,6 +156,7 @@ PROTOTYPES = {
     "linon_render_views_plain": (C.c_int, [vp, vp, i32, vp, i32]),
     "linon_autotune_batch": (C.c_int, [vp, vp, i32, vp, i32, P(BatchTuning), P(C.c_double)]),
     "linon_probe_fp32_peak": (C.c_int, [vp, P(C.c_double)]),
+    "linon_check_bounded_wait": (C.c_int, [vp, i32]),
     "linon_serve_start": (C.c_int, [vp, vp, i32, P(ServeConfig), P(vp)]),
     "linon_serve_submit": (C.c_int, [vp, P(Request), P(C.c_uint64)]),
     "linon_serve_poll": (C.c_int, [vp, C.c_uint64, P(Result)]),

@@ -39,7 +39,7 @@ CPP_SOURCES = [
     "runtime/serve.cpp",
     "runtime/obj.cpp",
 ]
-CU_SOURCES = ["runtime/kernels.cu", "runtime/noalloc.cu", "runtime/grid.cu"]
+CU_SOURCES = ["runtime/kernels.cu", "runtime/noalloc.cu", "runtime/grid.cu", "runtime/selfcheck.cu"]
 GENERATED = BUILD_DIR / "embedded_sources.cpp"
 
 CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",

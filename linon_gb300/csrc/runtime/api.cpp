@@ -979,6 +979,15 @@ int linon_outline_indices(uint16_t* out, size_t cap) {
   return int(n);
 }
 
+int linon_check_bounded_wait(linon_ctx* ctx, int32_t polls) {
+  LINON_TRY_BEGIN
+  if (int st = enter(ctx)) return st;
+  if (polls < 1 || polls > (1 << 24)) return set_error(LINON_EINVAL, "polls must be in [1, 2^24]");
+  LINON_CUDA(launch_bounded_wait_check(ctx->d_err, polls, ctx->stream));
+  return linon_synchronize(ctx);
+  LINON_TRY_END
+}
+
 int linon_probe_fp32_peak(linon_ctx* ctx, double* tflops) {
   LINON_TRY_BEGIN
   if (int st = enter(ctx)) return st;

@@ -45,6 +45,9 @@ cudaError_t launch_quantile_hist(const float* e, int W, int H, int border, unsig
 cudaError_t launch_pack_samples(const float4* pos, linon_ray_sample* out, int n_rays, int n_pts,
                                 cudaStream_t s);
 cudaError_t launch_fp32_probe(float* out, int blocks, int threads, int iters, cudaStream_t s);
+// One CTA waiting (at most `polls` polls) on an mbarrier nothing completes:
+// sets error bit 1 in *err (selfcheck.cu).
+cudaError_t launch_bounded_wait_check(int* err, int polls, cudaStream_t stream);
 cudaError_t launch_sum_steps(const int* steps, long long n, unsigned long long* out, cudaStream_t s);
 
 }  // namespace linon

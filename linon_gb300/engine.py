@@ -257,6 +257,11 @@ class Engine:
         check(self.lib.linon_probe_fp32_peak(self.ctx, C.byref(v)))
         return v.value
 
+    def check_bounded_wait(self, polls: int = 4096) -> int:
+        """linon_check_bounded_wait: the raw status (LINON_ETIMEOUT when the
+        device's bounded wait ran out and was reported)."""
+        return int(self.lib.linon_check_bounded_wait(self.ctx, int(polls)))
+
 
 def predefined_source(fid: int) -> str:
     s = load().linon_predefined_source(int(fid))

@@ -552,6 +552,28 @@ def test_batch_graph_replay_and_tuning(engine):
         assert np.percentile(d[same], 99) <= 1e-4
 
 
+def test_bounded_device_wait_reports_timeout(engine):
+    """Failure path of the bounded mbarrier wait: one CTA waits on a barrier
+    nothing completes; the wait runs out after its poll budget, the kernel
+    flags it and returns, the host reads LINON_ETIMEOUT, and the context
+    renders normally afterwards (the error word is cleared)."""
+    import time
+    t0 = time.perf_counter()
+    assert engine.check_bounded_wait(2000) == _abi.LINON_ETIMEOUT
+    assert time.perf_counter() - t0 < 10.0
+    assert "flags 1" in engine.lib.linon_last_error().decode()
+    assert engine.lib.linon_synchronize(engine.ctx) == _abi.LINON_OK
+    with pytest.raises(_abi.LinonError):
+        _abi.check(engine.check_bounded_wait(0))  # polls out of range
+    w = wl.plain_small(32, 24)
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    fld = field(engine, "twist", True)
+    planes = FramePlanes.allocate(w.width, w.height)
+    engine.render(fld, w.camera, w.settings, wl.fixed_steps(0.05, 20), planes)
+    engine.synchronize()
+    assert int(planes.steps.sum().item()) == 20 * 32 * 24
+
+
 def test_hbm_budget_admission():
     from linon_gb300 import Engine
     e = Engine(0, hbm_budget=1 << 20)
