@@ -45,6 +45,7 @@ struct Ty {
   Cat ecat = Void;
   int alen = 0;
   int sid = -1;  // struct (or array-of-struct element) index
+  int eid = -1;  // arrays of arrays: the element type (index into g_arr_elems)
 };
 
 // Struct declarations of the module being translated (one translation per
@@ -56,6 +57,9 @@ struct StructDef {
   std::string cpp;  // built-in result structs (frexp, modf): the runtime's type
 };
 thread_local std::vector<StructDef>* g_structs = nullptr;
+// Element types of arrays whose elements are arrays (one entry per distinct
+// type, so equal types share an index).
+thread_local std::vector<Ty>* g_arr_elems = nullptr;
 int struct_id(const std::string& n) {
   if (!g_structs) return -1;
   for (size_t i = 0; i < g_structs->size(); ++i)
@@ -67,24 +71,44 @@ Ty scalar(SK s) { Ty t; t.cat = Ty::Scalar; t.s = s; return t; }
 Ty vecT(SK s, int n) { Ty t; t.cat = Ty::Vec; t.s = s; t.n = n; return t; }
 Ty matT(int c, int r) { Ty t; t.cat = Ty::Mat; t.s = SK::F32; t.n = c; t.r = r; return t; }
 Ty voidT() { return Ty(); }
+bool operator==(const Ty& a, const Ty& b) {
+  return a.cat == b.cat && (a.cat == Ty::Void || (a.s == b.s && a.n == b.n && a.r == b.r && a.ecat == b.ecat &&
+                                                  a.alen == b.alen && a.sid == b.sid && a.eid == b.eid));
+}
+int intern_elem(const Ty& el) {
+  for (size_t i = 0; i < g_arr_elems->size(); ++i)
+    if ((*g_arr_elems)[i] == el) return int(i);
+  g_arr_elems->push_back(el);
+  return int(g_arr_elems->size()) - 1;
+}
 Ty arrT(const Ty& el, int len) {
+  if (el.cat == Ty::Arr) {  // array of arrays: the element type by reference
+    Ty t;
+    t.cat = Ty::Arr;
+    t.ecat = Ty::Arr;
+    t.alen = len;
+    t.eid = intern_elem(el);
+    return t;
+  }
   Ty t = el;
   t.ecat = el.cat;
   t.cat = Ty::Arr;
   t.alen = len;
+  t.eid = -1;
   return t;
 }
 Ty elemT(const Ty& a) {
+  if (a.ecat == Ty::Arr) return (*g_arr_elems)[size_t(a.eid)];
   Ty t = a;
   t.cat = a.ecat;
   t.ecat = Ty::Void;
   t.alen = 0;
   return t;
 }
-
-bool operator==(const Ty& a, const Ty& b) {
-  return a.cat == b.cat && (a.cat == Ty::Void || (a.s == b.s && a.n == b.n && a.r == b.r && a.ecat == b.ecat &&
-                                                  a.alen == b.alen && a.sid == b.sid));
+// the struct at the bottom of nested arrays (or the struct itself), or -1
+int inner_struct(Ty t) {
+  while (t.cat == Ty::Arr) t = elemT(t);
+  return t.cat == Ty::Struct ? t.sid : -1;
 }
 bool operator!=(const Ty& a, const Ty& b) { return !(a == b); }
 
@@ -156,12 +180,15 @@ SK concrete_sk(SK s) {
   return s;
 }
 Ty concretize(Ty t) {
+  if (t.cat == Ty::Arr && t.ecat == Ty::Arr) return arrT(concretize(elemT(t)), t.alen);
   if (t.cat == Ty::Scalar || t.cat == Ty::Vec || t.cat == Ty::Arr) t.s = concrete_sk(t.s);
   return t;
 }
 bool ty_convertible(const Ty& from, const Ty& to) {
   if (from.cat != to.cat) return false;
   if (from.cat == Ty::Struct) return from.sid == to.sid;
+  if (from.cat == Ty::Arr && (from.ecat == Ty::Arr || to.ecat == Ty::Arr))
+    return from.alen == to.alen && from.ecat == to.ecat && ty_convertible(elemT(from), elemT(to));
   if (from.cat == Ty::Arr)
     return from.alen == to.alen && from.ecat == to.ecat && from.n == to.n && from.r == to.r &&
            from.sid == to.sid && convertible(from.s, to.s);
@@ -594,7 +621,6 @@ class Parser {
       // array<E, N>: E a scalar, vector or matrix type, N an integer literal
       expect("<");
       Ty e = type();
-      if (e.cat == Ty::Arr) fail(k.line, k.col, "arrays of arrays are not supported in field functions");
       if (e.cat == Ty::Void) fail(k.line, k.col, "invalid array element type");
       if (is_p(">") || is_p(">>") || is_p(">="))
         fail(cur().line, cur().col, "runtime-sized arrays are not allowed in a function; give the element count");
@@ -1614,6 +1640,11 @@ class Compiler {
         Ty el = e.args[0]->ty;
         for (auto& a : e.args) {
           const Ty& at = a->ty;
+          if (at.cat == Ty::Arr || at.cat == Ty::Struct) {  // arrays of arrays / of structs
+            if (!(concretize(at) == concretize(el)))
+              fail(a->line, a->col, "array elements of different types: " + wgsl_name(el) + " and " + wgsl_name(at));
+            continue;
+          }
           if (at.cat != Ty::Scalar && at.cat != Ty::Vec && at.cat != Ty::Mat)
             fail(a->line, a->col, "invalid array element " + wgsl_name(at));
           if (at.cat != el.cat || at.n != el.n || at.r != el.r)
@@ -2697,10 +2728,15 @@ Translation translate(const std::string& field_body, const std::string& helpers_
   const std::string module = helpers_src + "\n" + header + field_body + "\n}\n";
   const int body_first_line = count_lines(helpers_src) + 3;  // 1-based line of the body
   std::vector<StructDef> structs;
+  std::vector<Ty> arr_elems;
   struct Reset {
-    ~Reset() { g_structs = nullptr; }
+    ~Reset() {
+      g_structs = nullptr;
+      g_arr_elems = nullptr;
+    }
   } reset;
   g_structs = &structs;
+  g_arr_elems = &arr_elems;
   try {
     Parser ps(lex(module));
     Compiler cc;
@@ -2714,7 +2750,7 @@ Translation translate(const std::string& field_body, const std::string& helpers_
       if (state[size_t(i)] == 1) throw CompileError(d.line, d.col, "struct '" + d.name + "' contains itself");
       state[size_t(i)] = 1;
       for (auto& m : d.members)
-        if ((m.second.cat == Ty::Struct || m.second.ecat == Ty::Struct) && m.second.sid >= 0) visit(m.second.sid);
+        if (inner_struct(m.second) >= 0) visit(inner_struct(m.second));
       state[size_t(i)] = 2;
       order.push_back(i);
     };

@@ -372,7 +372,6 @@ def test_arrays_semantics():
     ("let a = array(1.0, vec2<f32>(1.0)); return p;", "different types"),
     ("let a = array<f32, 3>(1.0, 2.0, 3.0); return vec3<f32>(a[3]);", "index out of bounds"),
     ("var a: array<f32>; return p;", "runtime-sized arrays"),
-    ("var a: array<array<f32, 2>, 2>; return p;", "arrays of arrays"),
     ("let n = 3; var a: array<f32, n>; return p;", "integer literal"),
     ("let a = array<f32, 2>(); let b = a + a; return p;", "cannot be applied to arrays"),
     ("let a = array<f32, 2>(); return vec3<f32>(abs(a)[0]);", "does not take an array"),
@@ -837,3 +836,60 @@ return unpack4x8snorm(u).xyz + unpack4x8unorm(u).xyz + vec3<f32>(unpack2x16float
         both_nan = (np.isnan(dev) & np.isnan(host)) if k == 2 else np.zeros(dev.shape, bool)
         np.testing.assert_array_equal(np.where(both_nan, 0, dev.view(np.uint32)),
                                       np.where(both_nan, 0, host.view(np.uint32)))
+
+
+NESTED_HELPERS = """
+struct Cell { w: f32, k: array<i32, 2> }
+alias Grid = array<array<f32, 3>, 2>;
+fn total(g: Grid) -> f32 {
+    var s = 0.0;
+    for (var i = 0; i < 2; i++) { for (var j = 0; j < 3; j++) { s += g[i][j]; } }
+    return s;
+}
+"""
+
+NESTED_BODY = """
+var g: Grid;                                         // zero value
+g[1][2] = p.x;
+g[0] = array<f32, 3>(1.0, p.y, 3.0);
+let h = g;                                           // value copy
+g[0][0] = 100.0;
+let m = array(array(p.z, 2.0), array(4.0, v.x));     // inferred, abstract literals made f32
+var cells = array<array<Cell, 2>, 2>();
+cells[1][0] = Cell(t, array<i32, 2>(3, 4));
+cells[1][0].k[1] = 7;
+let i = i32(t) % 4;                                  // runtime index, clamped to [0, 1]
+return vec3<f32>(total(h), m[1][1] + m[0][0] + m[i][1], cells[1][0].w + f32(cells[1][0].k[1]) + g[0][0]);
+"""
+
+
+def test_arrays_of_arrays_semantics():
+    """array<array<T, N>, M>: zero values, element and row assignment, value
+    copies, inferred nested constructors, arrays of structs in arrays,
+    clamped runtime indices, aliases, function parameters."""
+    rng = np.random.default_rng(9)
+    x = rng.uniform(-2, 2, (24, 13)).astype(np.float32)
+    x[:, 12] = rng.integers(-3, 9, 24).astype(np.float32)
+    out = _host_eval(NESTED_BODY, x, NESTED_HELPERS)
+    p, v, t = x[:, 3:6], x[:, 9:12], x[:, 12]
+    total = ((np.float32(1.0) + p[:, 1]) + np.float32(3.0)) + np.float32(0) + np.float32(0) + p[:, 0]
+    idx = np.clip(np.fmod(t.astype(np.int32), 4), 0, 1)
+    m = np.stack([np.stack([p[:, 2], np.full(24, 2.0, np.float32)], -1),
+                  np.stack([np.full(24, 4.0, np.float32), v[:, 0]], -1)], 1)
+    col1 = m[np.arange(24), idx, 1]
+    want = np.stack([total.astype(np.float32), (v[:, 0] + p[:, 2]) + col1, (t + np.float32(7.0)) + np.float32(100.0)], -1)
+    np.testing.assert_allclose(out, want.astype(np.float32), rtol=0, atol=1e-6)
+    assert "linon_march_v1" in validate_field(NESTED_BODY, NESTED_HELPERS)
+    code = translate_wgsl(NESTED_BODY, NESTED_HELPERS)
+    assert "::wgsl::arr<::wgsl::arr<float,3>,2>" in code
+
+
+@pytest.mark.parametrize("body,needle", [
+    ("let a = array(array(1.0, 2.0), array(1.0, 2.0, 3.0)); return p;", "array elements of different types"),
+    ("var a: array<array<f32, 2>, 2>; a[0] = array<f32, 3>(1.0, 2.0, 3.0); return p;", "cannot assign"),
+    ("var a: array<array<f32, 2>, 2>; let b = a[0][2]; return p;", "index out of bounds"),
+])
+def test_nested_array_diagnostics(body, needle):
+    with pytest.raises(_abi.LinonCompileError) as e:
+        translate_wgsl(body)
+    assert needle in e.value.message, e.value.message
