@@ -36,7 +36,7 @@ namespace {
 enum class SK { Bool, I32, U32, F32, AInt, AFloat };
 
 struct Ty {
-  enum Cat { Void, Scalar, Vec, Mat, Arr, Struct } cat = Void;
+  enum Cat { Void, Scalar, Vec, Mat, Arr, Struct, Ptr } cat = Void;  // Ptr: ptr<function, T>
   SK s = SK::F32;
   int n = 0;  // vector size / matrix columns (of the element, for arrays)
   int r = 0;  // matrix rows (of the element, for arrays)
@@ -45,7 +45,7 @@ struct Ty {
   Cat ecat = Void;
   int alen = 0;
   int sid = -1;  // struct (or array-of-struct element) index
-  int eid = -1;  // arrays of arrays: the element type (index into g_arr_elems)
+  int eid = -1;  // arrays of arrays: the element type; pointers: the pointee (g_arr_elems)
 };
 
 // Struct declarations of the module being translated (one translation per
@@ -105,6 +105,13 @@ Ty elemT(const Ty& a) {
   t.alen = 0;
   return t;
 }
+Ty ptrT(const Ty& pointee) {
+  Ty t;
+  t.cat = Ty::Ptr;
+  t.eid = intern_elem(pointee);
+  return t;
+}
+Ty pointeeT(const Ty& p) { return (*g_arr_elems)[size_t(p.eid)]; }
 // the struct at the bottom of nested arrays (or the struct itself), or -1
 int inner_struct(Ty t) {
   while (t.cat == Ty::Arr) t = elemT(t);
@@ -135,6 +142,7 @@ std::string wgsl_name(const Ty& t) {
     case Ty::Vec: return "vec" + std::to_string(t.n) + "<" + sk_name(t.s) + ">";
     case Ty::Mat: return "mat" + std::to_string(t.n) + "x" + std::to_string(t.r) + "<f32>";
     case Ty::Arr: return "array<" + wgsl_name(elemT(t)) + ", " + std::to_string(t.alen) + ">";
+    case Ty::Ptr: return "ptr<function, " + wgsl_name(pointeeT(t)) + ">";
     case Ty::Struct: return g_structs && t.sid >= 0 ? (*g_structs)[size_t(t.sid)].name : "struct";
   }
   return "?";
@@ -155,6 +163,7 @@ std::string cpp_name(const Ty& t) {
     case Ty::Vec: return std::string("::wgsl::vec<") + sk_cpp(t.s) + "," + std::to_string(t.n) + ">";
     case Ty::Mat: return "::wgsl::mat<" + std::to_string(t.n) + "," + std::to_string(t.r) + ">";
     case Ty::Arr: return "::wgsl::arr<" + cpp_name(elemT(t)) + "," + std::to_string(t.alen) + ">";
+    case Ty::Ptr: return cpp_name(pointeeT(t)) + "&";
     case Ty::Struct:
       if (g_structs && t.sid >= 0 && !(*g_structs)[size_t(t.sid)].cpp.empty()) return (*g_structs)[size_t(t.sid)].cpp;
       return "s_" + (g_structs && t.sid >= 0 ? (*g_structs)[size_t(t.sid)].name : std::string("?"));
@@ -187,6 +196,7 @@ Ty concretize(Ty t) {
 bool ty_convertible(const Ty& from, const Ty& to) {
   if (from.cat != to.cat) return false;
   if (from.cat == Ty::Struct) return from.sid == to.sid;
+  if (from.cat == Ty::Ptr) return from.eid == to.eid;
   if (from.cat == Ty::Arr && (from.ecat == Ty::Arr || to.ecat == Ty::Arr))
     return from.alen == to.alen && from.ecat == to.ecat && ty_convertible(elemT(from), elemT(to));
   if (from.cat == Ty::Arr)
@@ -562,6 +572,7 @@ class Parser {
       Ty t = type();
       if (t.cat == Ty::Struct && t.sid == struct_id(name))
         fail(mt.line, mt.col, "struct '" + name + "' cannot contain itself");
+      if (t.cat == Ty::Ptr) fail(mt.line, mt.col, "a struct member cannot be a pointer");
       d.members.push_back({m, t});
       if (!accept(",")) break;
     }
@@ -583,6 +594,23 @@ class Parser {
     if (n == "u32") return scalar(SK::U32);
     if (n == "bool") return scalar(SK::Bool);
     if (n == "f16" || n == "f64") fail(k.line, k.col, "type '" + n + "' is not supported");
+    if (n == "ptr") {
+      // ptr<function, T[, read_write]>: function-space pointers only
+      expect("<");
+      Tok sp = cur();
+      const std::string space = ident("address space");
+      if (space != "function")
+        fail(sp.line, sp.col, "only ptr<function, T> is supported in field functions, found address space '" + space + "'");
+      expect(",");
+      Ty pt = type();
+      if (pt.cat == Ty::Ptr) fail(k.line, k.col, "pointers to pointers are not allowed");
+      if (accept(",")) {
+        Tok am = cur();
+        if (ident("access mode") != "read_write") fail(am.line, am.col, "function-space pointers are read_write");
+      }
+      close_template();
+      return ptrT(pt);
+    }
     Ty t;
     if (alias_type(n, t)) return t;
     auto ua = aliases_.find(n);
@@ -622,6 +650,7 @@ class Parser {
       expect("<");
       Ty e = type();
       if (e.cat == Ty::Void) fail(k.line, k.col, "invalid array element type");
+      if (e.cat == Ty::Ptr) fail(k.line, k.col, "an array element cannot be a pointer");
       if (is_p(">") || is_p(">>") || is_p(">="))
         fail(cur().line, cur().col, "runtime-sized arrays are not allowed in a function; give the element count");
       expect(",");
@@ -677,7 +706,9 @@ class Parser {
     if (accept("->")) {
       skip_attributes();
       f->has_ret = true;
+      Tok rt = cur();
       f->ret = type();
+      if (f->ret.cat == Ty::Ptr) fail(rt.line, rt.col, "a function cannot return a pointer");
     }
     f->body = block();
     return f;
@@ -980,7 +1011,13 @@ class Parser {
       e->args.push_back(unary());
       return e;
     }
-    if (is_p("&") || is_p("*")) fail(cur().line, cur().col, "pointers are not supported in field functions");
+    if (is_p("&") || is_p("*")) {  // address-of / indirection (function-space pointers)
+      Tok at = next();
+      EP e = mkE(Expr::Unary, at);
+      e->op = at.s;
+      e->args.push_back(unary());
+      return e;
+    }
     return postfix(primary());
   }
   EP postfix(EP e) {
@@ -1294,6 +1331,24 @@ class Compiler {
     check(a);
     e.fl = a.fl;
     e.tr = a.tr;
+    if (e.op == "&") {
+      // the address of a variable (or of a part of one other than a vector
+      // component): a ptr<function, T>
+      if (!(a.lv && a.mut)) fail(e.line, e.col, "'&' needs a variable (a 'var' or a part of one)");
+      if ((a.kind == Expr::Member || a.kind == Expr::Index) && a.args[0]->ty.cat == Ty::Vec)
+        fail(e.line, e.col, "cannot take the address of a vector component");
+      if (a.ty.cat == Ty::Ptr) fail(e.line, e.col, "pointers to pointers are not allowed");
+      e.ty = ptrT(a.ty);
+      return;
+    }
+    if (e.op == "*") {
+      if (a.ty.cat != Ty::Ptr) fail(e.line, e.col, "'*' needs a pointer, found " + wgsl_name(a.ty));
+      e.ty = pointeeT(a.ty);
+      e.lv = true;
+      e.mut = true;  // function-space pointers are read_write
+      return;
+    }
+    if (a.ty.cat == Ty::Ptr) fail(e.line, e.col, "operator '" + e.op + "' cannot be applied to a pointer");
     if (a.ty.cat == Ty::Arr) fail(e.line, e.col, "operator '" + e.op + "' cannot be applied to an array");
     if (a.ty.cat == Ty::Struct) fail(e.line, e.col, "operator '" + e.op + "' cannot be applied to a struct");
     if (e.op == "-") {
@@ -1471,9 +1526,20 @@ class Compiler {
     return -1;
   }
 
+  // p.m and p[i] on a pointer p access its pointee (WGSL's pointer
+  // composite access); the pointer is a C++ reference, so nothing changes in
+  // the emitted code
+  static void deref_in_place(Expr& a) {
+    if (a.ty.cat != Ty::Ptr) return;
+    a.ty = pointeeT(a.ty);
+    a.lv = true;
+    a.mut = true;
+  }
+
   void check_member(Expr& e) {
     Expr& a = *e.args[0];
     check(a);
+    deref_in_place(a);
     e.fl = a.fl;
     e.tr = a.tr;
     if (a.ty.cat == Ty::Struct) {
@@ -1510,6 +1576,7 @@ class Compiler {
     Expr& a = *e.args[0];
     Expr& i = *e.args[1];
     check(a);
+    deref_in_place(a);
     check(i);
     e.fl = a.fl + i.fl;
     e.tr = a.tr + i.tr;
@@ -1774,6 +1841,17 @@ class Compiler {
       if (!(a.ty == f.params[i].ty || ty_convertible(a.ty, f.params[i].ty)))
         fail(a.line, a.col, "argument " + std::to_string(i + 1) + " of '" + f.name + "': expected " + wgsl_name(f.params[i].ty) + ", found " + wgsl_name(a.ty));
       ci.targets.push_back(f.params[i].ty);
+    }
+    // two pointer arguments into the same variable would alias (WGSL rejects
+    // such a call): compare the roots of the '&' arguments
+    std::set<std::string> roots;
+    for (auto& a : e.args) {
+      if (a->ty.cat != Ty::Ptr || a->kind != Expr::Unary) continue;
+      const Expr* r = a->args[0].get();
+      while (r->kind == Expr::Member || r->kind == Expr::Index || (r->kind == Expr::Unary && r->op == "*"))
+        r = r->args[0].get();
+      if (r->kind == Expr::Name && !roots.insert(r->op).second)
+        fail(a->line, a->col, "two pointer arguments of '" + f.name + "' refer to '" + r->op + "' (aliasing)");
     }
     ci.fn = "u_" + f.name;
     e.ty = f.has_ret ? f.ret : voidT();
@@ -2219,6 +2297,8 @@ class Compiler {
       }
       case Expr::Unary:
         if (e.cst) return lit_as(e.cv, concretize(e.ty), e.line, e.col);
+        // a pointer is a C++ reference: &x and *p are the reference itself
+        if (e.op == "&" || e.op == "*") return ex(*e.args[0]);
         return "(" + e.op + ex(*e.args[0]) + ")";
       case Expr::Binary: {
         if (e.cst) return lit_as(e.cv, concretize(e.ty), e.line, e.col);
@@ -2395,6 +2475,8 @@ class Compiler {
           cv = s.e->cv;
           t = s.e->ty;
         }
+        if (t.cat == Ty::Ptr && s.kind != Stmt::Let)
+          fail(s.line, s.col, "a pointer can only be declared with 'let'");
         init = s.e ? ex_as(*s.e, concretize(t)) : cpp_name(t) + "()";
         Sym sym;
         sym.ty = cst ? t : concretize(t);
@@ -2403,7 +2485,9 @@ class Compiler {
         sym.cst = cst;
         sym.cv = cv;
         if (!cst) {
-          out += ind(d) + (sym.is_var ? "" : "const ") + cpp_name(sym.ty) + " " + sym.cpp + " = " + init + ";\n";
+          // a pointer binds a (non-const) C++ reference to the variable
+          const bool konst = !sym.is_var && sym.ty.cat != Ty::Ptr;
+          out += ind(d) + (konst ? "const " : "") + cpp_name(sym.ty) + " " + sym.cpp + " = " + init + ";\n";
         }
         declare(s.name, sym, s.line, s.col);
         return;

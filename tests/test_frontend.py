@@ -893,3 +893,82 @@ def test_nested_array_diagnostics(body, needle):
     with pytest.raises(_abi.LinonCompileError) as e:
         translate_wgsl(body)
     assert needle in e.value.message, e.value.message
+
+
+POINTER_HELPERS = """
+fn split(x: f32, whole: ptr<function, f32>, frac: ptr<function, f32>) {
+    *whole = floor(x);
+    *frac = x - *whole;
+}
+fn bump(v: ptr<function, vec3<f32>>, k: f32) {
+    (*v).y += k;
+    v.z = v.x * 2.0;                 // pointer composite access
+}
+fn fill(a: ptr<function, array<f32, 3>>, s: f32) {
+    for (var i = 0; i < 3; i++) { a[i] = s * f32(i); }
+}
+struct Acc { sum: f32, n: i32 }
+fn add(acc: ptr<function, Acc>, x: f32) {
+    acc.sum += x;
+    (*acc).n = (*acc).n + 1;
+}
+"""
+
+POINTER_BODY = """
+var w = 0.0;
+var f = 0.0;
+split(p.x * 3.0, &w, &f);
+var q = v;
+bump(&q, t);
+let r = &q;
+r.x = (*r).x + 1.0;
+var arr: array<f32, 3>;
+fill(&arr, w);
+var acc = Acc(0.0, 0);
+add(&acc, f);
+add(&acc, arr[2]);
+var s = array<Acc, 2>();
+add(&s[1], 5.0);
+return vec3<f32>(w + f, q.y + q.z + q.x, acc.sum + f32(acc.n) + s[1].sum);
+"""
+
+
+def test_pointer_semantics():
+    """ptr<function, T> parameters (out-parameters), '&' of variables and of
+    parts of them, '*' and WGSL's pointer composite access, a pointer bound
+    with 'let'."""
+    rng = np.random.default_rng(12)
+    x = rng.uniform(-2, 2, (20, 13)).astype(np.float32)
+    out = _host_eval(POINTER_BODY, x, POINTER_HELPERS)
+    p, v, t = x[:, 3:6], x[:, 9:12], x[:, 12]
+    y = p[:, 0] * np.float32(3.0)
+    w = np.floor(y)
+    f = y - w
+    q = v.copy()
+    q[:, 1] = q[:, 1] + t
+    q[:, 2] = q[:, 0] * np.float32(2.0)
+    q[:, 0] = q[:, 0] + np.float32(1.0)
+    a2 = w * np.float32(2.0)
+    acc = (np.float32(0.0) + f) + a2
+    want = np.stack([w + f, (q[:, 1] + q[:, 2]) + q[:, 0], (acc + np.float32(2.0)) + np.float32(5.0)], -1)
+    np.testing.assert_array_equal(out, want.astype(np.float32))
+    assert "linon_march_v1" in validate_field(POINTER_BODY, POINTER_HELPERS)
+
+
+@pytest.mark.parametrize("helpers,body,needle", [
+    ("", "let a = 1.0; let q = &a; return p;", "needs a variable"),
+    ("", "var a = p; let q = &a.x; return p;", "vector component"),
+    ("", "var a = 1.0; var q = &a; return p;", "only be declared with 'let'"),
+    ("", "let a = *p; return p;", "'*' needs a pointer"),
+    ("fn f(x: ptr<function, f32>) -> ptr<function, f32> { return x; }", "return p;", "cannot return a pointer"),
+    ("struct S { a: ptr<function, f32> }", "return p;", "struct member cannot be a pointer"),
+    ("fn f(x: array<ptr<function, f32>, 2>) {}", "return p;", "array element cannot be a pointer"),
+    ("fn f(x: ptr<private, f32>) {}", "return p;", "only ptr<function, T>"),
+    ("fn f(x: ptr<function, f32>, y: ptr<function, f32>) { *x = *y; }",
+     "var a = 1.0; f(&a, &a); return p;", "aliasing"),
+    ("fn f(x: ptr<function, f32>) {}", "var a = 1; f(&a); return p;", "expected ptr<function, f32>"),
+])
+def test_pointer_diagnostics(helpers, body, needle):
+    with pytest.raises(_abi.LinonCompileError) as e:
+        translate_wgsl(body, helpers or None)
+    assert needle in e.value.message, e.value.message
