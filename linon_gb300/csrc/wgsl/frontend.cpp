@@ -385,7 +385,7 @@ struct Stmt;
 using SP = std::unique_ptr<Stmt>;
 struct Stmt {
   enum Kind { Let, Var, Const, Assign, Compound, Incr, Decr, Phony, ExprS, If, For, While, Loop,
-              Break, Continue, Return, Block, BreakIf, Switch } kind = ExprS;
+              Break, Continue, Return, Block, BreakIf, Switch, ConstAssert } kind = ExprS;
   int line = 0, col = 0;
   std::string name, op;
   bool has_ty = false;
@@ -423,6 +423,7 @@ struct GConst {
   std::string name;
   int line = 0, col = 0;
   bool is_override = false;  // `override`: the default value, a concrete scalar
+  bool is_assert = false;    // module-scope const_assert (no name, no value)
   bool has_ty = false;
   Ty ty;
   EP e;
@@ -481,6 +482,45 @@ class Parser {
         g->e = expr();
         expect(";");
         consts.push_back(std::move(g));
+      } else if (is_kw("const_assert")) {
+        Tok k = next();
+        auto g = std::make_unique<GConst>();
+        g->line = k.line;
+        g->col = k.col;
+        g->is_assert = true;
+        g->e = expr();
+        expect(";");
+        consts.push_back(std::move(g));
+      } else if (is_kw("diagnostic")) {
+        // diagnostic(severity, rule); — the front end reports no
+        // uniformity diagnostics, so the filter has nothing to change
+        next();
+        expect("(");
+        Tok sv = cur();
+        const std::string sev = ident("diagnostic severity");
+        if (sev != "error" && sev != "warning" && sev != "info" && sev != "off")
+          fail(sv.line, sv.col, "unknown diagnostic severity '" + sev + "'");
+        expect(",");
+        ident("diagnostic rule");
+        while (accept(".")) ident("diagnostic rule");
+        accept(",");
+        expect(")");
+        expect(";");
+      } else if (is_kw("requires")) {
+        // language extensions: the ones WGSL defines are all satisfied here
+        // (or concern resources a field function cannot use)
+        next();
+        static const std::set<std::string> known = {"readonly_and_readwrite_storage_textures",
+                                                    "packed_4x8_integer_dot_product",
+                                                    "unrestricted_pointer_parameters", "pointer_composite_access"};
+        for (;;) {
+          Tok xt = cur();
+          const std::string x = ident("language extension");
+          if (!known.count(x)) fail(xt.line, xt.col, "unknown language extension '" + x + "'");
+          if (!accept(",")) break;
+          if (is_p(";")) break;
+        }
+        expect(";");
       } else if (is_kw("alias")) {
         next();
         ident("alias name");
@@ -745,6 +785,13 @@ class Parser {
     }
     if (is_kw("let") || is_kw("var") || is_kw("const")) {
       SP s = decl();
+      expect(";");
+      return s;
+    }
+    if (is_kw("const_assert")) {
+      next();
+      SP s = mk(Stmt::ConstAssert, at);
+      s->e = expr();
       expect(";");
       return s;
     }
@@ -1168,6 +1215,7 @@ class Compiler {
       fmap[f->name] = f.get();
     }
     for (auto& c : consts) {
+      if (c->is_assert) continue;
       if (fmap.count(c->name) || cmap.count(c->name) || is_helper(c->name) || c->name == "PI")
         fail(c->line, c->col, "redefinition of '" + c->name + "'");
       cmap[c->name] = c.get();
@@ -1220,10 +1268,68 @@ class Compiler {
     scopes.back()[n] = s;
   }
 
+  // The value of a constant boolean expression: bool literals, '!', '&&',
+  // '||', '==' / '!=' of booleans, and comparisons of folded numbers.
+  bool const_bool(Expr& e, bool& val) {
+    if (e.kind == Expr::Lit && e.lit == 3) {
+      val = e.bval;
+      return true;
+    }
+    if (e.kind == Expr::Unary && e.op == "!") {
+      bool v;
+      if (!const_bool(*e.args[0], v)) return false;
+      val = !v;
+      return true;
+    }
+    if (e.kind != Expr::Binary) return false;
+    const std::string& op = e.op;
+    Expr& L = *e.args[0];
+    Expr& R = *e.args[1];
+    if (L.ty.cat == Ty::Scalar && L.ty.s == SK::Bool) {
+      bool a, b;
+      if (!const_bool(L, a) || !const_bool(R, b)) return false;
+      if (op == "&&" || op == "&") val = a && b;
+      else if (op == "||" || op == "|") val = a || b;
+      else if (op == "==") val = a == b;
+      else if (op == "!=") val = a != b;
+      else return false;
+      return true;
+    }
+    if (!(L.cst && R.cst && L.ty.cat == Ty::Scalar && R.ty.cat == Ty::Scalar)) return false;
+    const double a = L.cv, b = R.cv;
+    if (op == "<") val = a < b;
+    else if (op == "<=") val = a <= b;
+    else if (op == ">") val = a > b;
+    else if (op == ">=") val = a >= b;
+    else if (op == "==") val = a == b;
+    else if (op == "!=") val = a != b;
+    else return false;
+    return true;
+  }
+
+  void check_const_assert(Expr& e, int line, int col) {
+    check(e);
+    if (!(e.ty.cat == Ty::Scalar && e.ty.s == SK::Bool))
+      fail(line, col, "const_assert needs a bool expression, found " + wgsl_name(e.ty));
+    bool v = false;
+    if (!const_bool(e, v))
+      fail(line, col, "const_assert needs a constant expression (literals, abstract constants, comparisons, ! && ||)");
+    if (!v) fail(line, col, "const_assert failed");
+  }
+
   void check_gconst(GConst& g) {
     if (g.state == 2) return;
     if (g.state == 1) fail(g.line, g.col, "cyclic constant definition '" + g.name + "'");
     g.state = 1;
+    if (g.is_assert) {
+      auto saved = scopes;
+      scopes.clear();
+      scopes.emplace_back();
+      check_const_assert(*g.e, g.line, g.col);
+      scopes = saved;
+      g.state = 2;
+      return;
+    }
     auto saved = scopes;
     scopes.clear();
     scopes.emplace_back();
@@ -2711,6 +2817,9 @@ class Compiler {
         c.tr += worst.tr;
         return;
       }
+      case Stmt::ConstAssert:
+        check_const_assert(*s.e, s.line, s.col);
+        return;
       case Stmt::BreakIf:
         check(*s.e);
         if (!(s.e->ty.cat == Ty::Scalar && s.e->ty.s == SK::Bool)) fail(s.e->line, s.e->col, "'break if' condition must be bool");

@@ -972,3 +972,32 @@ def test_pointer_diagnostics(helpers, body, needle):
     with pytest.raises(_abi.LinonCompileError) as e:
         translate_wgsl(body, helpers or None)
     assert needle in e.value.message, e.value.message
+
+
+def test_const_assert_and_directives():
+    """const_assert at module and function scope (checked at translation,
+    no code), the diagnostic and requires directives, @diagnostic and
+    @must_use attributes."""
+    helpers = """
+requires pointer_composite_access, packed_4x8_integer_dot_product;
+diagnostic(off, derivative_uniformity);
+const N = 3;
+const_assert N > 2 && !(N == 4);
+const_assert 1.5 < 2.0;
+@must_use @diagnostic(warning, derivative_uniformity) fn twice(x: f32) -> f32 { return 2.0 * x; }
+"""
+    code = translate_wgsl("const_assert N * 2 == 6;\nconst_assert true || false;\nreturn p * twice(t);", helpers)
+    assert "const_assert" not in code and "u_twice" in code
+
+
+@pytest.mark.parametrize("helpers,body,needle", [
+    ("const_assert 1 > 2;", "return p;", "const_assert failed"),
+    ("", "const_assert p.x > 0.0; return p;", "needs a constant expression"),
+    ("", "const_assert 1; return p;", "needs a bool expression"),
+    ("requires no_such_extension;", "return p;", "unknown language extension"),
+    ("diagnostic(loud, derivative_uniformity);", "return p;", "unknown diagnostic severity"),
+])
+def test_const_assert_and_directive_diagnostics(helpers, body, needle):
+    with pytest.raises(_abi.LinonCompileError) as e:
+        translate_wgsl(body, helpers or None)
+    assert needle in e.value.message, e.value.message
