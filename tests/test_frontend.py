@@ -795,7 +795,8 @@ def test_new_builtins_device_equals_host(engine):
     """The device implementations of the bit, decomposition and packing
     builtins (CUDA integer intrinsics, ldexpf / frexpf / modff) give the
     host implementations' results bit for bit (precise module, through
-    linon_field_eval)."""
+    linon_field_eval); so do fields with pointers, arrays of arrays,
+    aliases and overrides."""
     import torch
     bodies = [
         # integer bits, as u32 bit patterns
@@ -826,7 +827,19 @@ return unpack4x8snorm(u).xyz + unpack4x8unorm(u).xyz + vec3<f32>(unpack2x16float
     x, _ = _bits_inputs(2048)
     rng = np.random.default_rng(31)
     x[:, 9:12] = rng.uniform(-3, 3, (len(x), 3)).astype(np.float32)
-    for k, body in enumerate(bodies):
+    cases = [(b, None) for b in bodies]
+    # pointers, arrays of arrays, aliases and overrides on the device (their
+    # x arguments are the float inputs, so give p finite values)
+    xf = x.copy()
+    xf[:, 3:6] = rng.uniform(-2, 2, (len(x), 3)).astype(np.float32)
+    cases += [(POINTER_BODY, POINTER_HELPERS), (NESTED_BODY, NESTED_HELPERS),
+              (ALIAS_OVERRIDE_BODY, ALIAS_OVERRIDE_HELPERS)]
+    for k, (body, helpers) in enumerate(cases):
+        if helpers is not None:
+            fld = engine.compile_field(body, helpers, precise=True)
+            dev = engine.field_eval(fld, torch.from_numpy(xf).cuda()).cpu().numpy()
+            np.testing.assert_array_equal(dev, _host_eval(body, xf, helpers))
+            continue
         fld = engine.compile_field(body, precise=True)
         dev = engine.field_eval(fld, torch.from_numpy(x).cuda()).cpu().numpy()
         host = _host_eval(body, x)
