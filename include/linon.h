@@ -243,6 +243,15 @@ int linon_wgsl_translate(const char* field_body, const char* helpers_src,
 int linon_render(linon_ctx* ctx, const linon_field* field,
                  const linon_camera* camera, const linon_settings* settings,
                  const linon_march_params* params, const linon_frame* out);
+/* Rows [row0, row1) of the same width x height frame (the primary rays of
+ * those rows, stored at their rows of `out`; other rows untouched): one
+ * shard of a frame split by rows across GPUs (no exchange; an overlay over
+ * a shard renders 2 * central_difference_delta halo rows on each inner
+ * side).                                                                    */
+int linon_render_rows(linon_ctx* ctx, const linon_field* field,
+                      const linon_camera* camera, const linon_settings* settings,
+                      const linon_march_params* params, const linon_frame* out,
+                      int32_t row0, int32_t row1);
 /* Evaluates the field at n points: in = n x 13 floats (p_prev.xyz, p.xyz,
  * v0.xyz, v.xyz, t), out = n x 3 floats; both device pointers.  This is the
  * field_function of main_view.wgsl:148 called on its own (field probes,

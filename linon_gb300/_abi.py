@@ -138,6 +138,7 @@ PROTOTYPES = {
     "linon_field_validate": (C.c_int, [cp, cp, C.c_int, C.c_char_p, sz]),
     "linon_wgsl_translate": (C.c_int, [cp, cp, C.c_char_p, sz, C.c_char_p, sz]),
     "linon_render": (C.c_int, [vp, vp, P(Camera), P(Settings), P(MarchParams), P(Frame)]),
+    "linon_render_rows": (C.c_int, [vp, vp, P(Camera), P(Settings), P(MarchParams), P(Frame), i32, i32]),
     "linon_field_eval": (C.c_int, [vp, vp, vp, vp, C.c_int64]),
     "linon_render_host": (C.c_int, [vp, vp, P(Camera), P(Settings), P(MarchParams), i32, i32,
                                     vp, vp, vp, vp]),

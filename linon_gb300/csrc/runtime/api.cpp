@@ -704,6 +704,20 @@ int linon_render(linon_ctx* ctx, const linon_field* field, const linon_camera* c
   LINON_TRY_END
 }
 
+int linon_render_rows(linon_ctx* ctx, const linon_field* field, const linon_camera* camera,
+                      const linon_settings* settings, const linon_march_params* params,
+                      const linon_frame* out, int32_t row0, int32_t row1) {
+  LINON_TRY_BEGIN
+  if (int st = enter(ctx)) return st;
+  if (!out) return set_error(LINON_EINVAL, "null frame");
+  if (int st = render_checks(ctx, field, camera, params, out->width, out->height)) return st;
+  if (row0 < 0 || row1 < row0 || row1 > out->height)
+    return set_error(LINON_EINVAL, "rows must satisfy 0 <= row0 <= row1 <= height");
+  if (row0 == row1) return LINON_OK;
+  return launch_rows(ctx, field, camera, settings, params, out, row0, row1, ctx->stream);
+  LINON_TRY_END
+}
+
 int linon_field_eval(linon_ctx* ctx, const linon_field* field, const float* in, float* out, int64_t n) {
   LINON_TRY_BEGIN
   if (int st = enter(ctx)) return st;

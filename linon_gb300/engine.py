@@ -159,6 +159,12 @@ class Engine:
         self._call("linon_render", self.ctx, field.handle, C.byref(camera), C.byref(settings),
                                     C.byref(params), C.byref(f))
 
+    def render_rows(self, field: Field, camera, settings, params, frame: FramePlanes, row0: int, row1: int):
+        """Rows [row0, row1) of the frame (linon_render_rows)."""
+        f = frame.abi()
+        self._call("linon_render_rows", self.ctx, field.handle, C.byref(camera), C.byref(settings),
+                   C.byref(params), C.byref(f), int(row0), int(row1))
+
     def field_eval(self, field: Field, inputs):
         """Evaluates the field at n points (torch CUDA tensor [n, 13]) -> [n, 3]."""
         import torch

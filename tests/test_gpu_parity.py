@@ -574,6 +574,44 @@ def test_bounded_device_wait_reports_timeout(engine):
     assert int(planes.steps.sum().item()) == 20 * 32 * 24
 
 
+def test_row_shards_equal_whole_frame(engine):
+    """One frame split by rows (sharding.shard_rows, halo 2 * delta): each
+    band rendered with linon_render_rows and overlaid alone gives the whole
+    frame's planes, overlay and exponents on its owned rows, bit for bit
+    (the bands run one after another on this GPU, each one rank's work)."""
+    from linon_gb300 import sharding
+    w = wl.lyapunov_1024(96, 80)
+    params = wl.fixed_steps(0.01, 100, kahan=True)
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    fld = field(engine, "lorenz_scaled", False)
+    delta = 2
+    st = wl.settings(overlay_mode=1, delta=delta, scaling=20.0)
+    full = FramePlanes.allocate(w.width, w.height)
+    engine.render(fld, w.camera, st, params, full)
+    t_full = torch.empty_like(full.color)
+    e_full = torch.zeros((w.height, w.width), dtype=torch.float32, device="cuda")
+    engine.overlay(st, w.width, w.height, full.color, full.mapping, t_full, e_full, fp64=True)
+    engine.synchronize()
+    ref = {k: getattr(full, k).cpu().numpy() for k in ("color", "mapping", "hit_id", "steps")}
+    t_ref, e_ref = t_full.cpu().numpy(), e_full.cpu().numpy()
+    for world in (2, 3):
+        for band in sharding.shard_rows(w.height, world, 2 * delta):
+            # each band with buffers of its own, as on its own rank (a band's
+            # overlay also writes its halo rows, with border values)
+            planes = FramePlanes.allocate(w.width, w.height)
+            tgt = torch.zeros_like(full.color)
+            ex = torch.zeros_like(e_full)
+            o0, o1 = sharding.overlay_band(engine, fld, w.camera, st, params, planes, tgt, ex, band)
+            engine.synchronize()
+            for k in ref:
+                np.testing.assert_array_equal(getattr(planes, k)[o0:o1].cpu().numpy(), ref[k][o0:o1])
+            np.testing.assert_array_equal(tgt[o0:o1].cpu().numpy(), t_ref[o0:o1])
+            np.testing.assert_array_equal(ex[o0:o1].cpu().numpy(), e_ref[o0:o1])
+    with pytest.raises(_abi.LinonError):
+        engine.render_rows(fld, w.camera, st, params, full, 10, 5)
+    engine.render_rows(fld, w.camera, st, params, full, 7, 7)  # empty range: nothing to do
+
+
 def test_hbm_budget_admission():
     from linon_gb300 import Engine
     e = Engine(0, hbm_budget=1 << 20)
