@@ -530,6 +530,46 @@ WG_BINARY(atan2, atan2f(a, b))
 WG_BINARY(step, (b >= a ? 1.0f : 0.0f))
 WG_BINARY(fmod_wgsl, (a - b * truncf(a / b)))
 #undef WG_BINARY
+// e1 % e2 with a scalar on one side (the scalar applies to every component)
+template <int N> WG_HD vec<float, N> fmod_wgsl(const vec<float, N>& a, float b) {
+  vec<float, N> r;
+  for (int i = 0; i < N; ++i) r[i] = fmod_wgsl(a[i], b);
+  return r;
+}
+template <int N> WG_HD vec<float, N> fmod_wgsl(float a, const vec<float, N>& b) {
+  vec<float, N> r;
+  for (int i = 0; i < N; ++i) r[i] = fmod_wgsl(a, b[i]);
+  return r;
+}
+
+// Integer division and remainder (WGSL 8.7): a / 0 = a, a % 0 = 0, and for
+// i32 the most negative value over -1 gives itself / 0 (no trap, no
+// undefined behaviour); otherwise truncating.
+WG_HD int div_int(int a, int b) { return (b == 0 || (a == -2147483647 - 1 && b == -1)) ? a : a / b; }
+WG_HD int mod_int(int a, int b) { return (b == 0 || (a == -2147483647 - 1 && b == -1)) ? 0 : a % b; }
+WG_HD unsigned div_int(unsigned a, unsigned b) { return b == 0u ? a : a / b; }
+WG_HD unsigned mod_int(unsigned a, unsigned b) { return b == 0u ? 0u : a % b; }
+// Shifts by the amount's low 5 bits; left shifts of i32 through u32 (no
+// signed overflow), right shifts of i32 arithmetic.
+WG_HD int shl(int a, unsigned b) { return int(unsigned(a) << (b & 31u)); }
+WG_HD unsigned shl(unsigned a, unsigned b) { return a << (b & 31u); }
+WG_HD int shr(int a, unsigned b) { return a >> (b & 31u); }
+WG_HD unsigned shr(unsigned a, unsigned b) { return a >> (b & 31u); }
+#define WG_INT_BINARY(NAME, BT)                                                              \
+  template <class T, int N> WG_HD vec<T, N> NAME(const vec<T, N>& a, const vec<BT, N>& b) { \
+    vec<T, N> r;                                                                             \
+    for (int i = 0; i < N; ++i) r[i] = NAME(a[i], b[i]);                                     \
+    return r;                                                                                \
+  }
+WG_INT_BINARY(div_int, T)
+WG_INT_BINARY(mod_int, T)
+WG_INT_BINARY(shl, unsigned)
+WG_INT_BINARY(shr, unsigned)
+#undef WG_INT_BINARY
+template <class T, int N> WG_HD vec<T, N> div_int(const vec<T, N>& a, T b) { return div_int(a, vec<T, N>(b)); }
+template <class T, int N> WG_HD vec<T, N> div_int(T a, const vec<T, N>& b) { return div_int(vec<T, N>(a), b); }
+template <class T, int N> WG_HD vec<T, N> mod_int(const vec<T, N>& a, T b) { return mod_int(a, vec<T, N>(b)); }
+template <class T, int N> WG_HD vec<T, N> mod_int(T a, const vec<T, N>& b) { return mod_int(vec<T, N>(a), b); }
 
 WG_HD float min(float a, float b) { return fmin_(a, b); }
 WG_HD float max(float a, float b) { return fmax_(a, b); }

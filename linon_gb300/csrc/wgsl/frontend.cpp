@@ -1549,6 +1549,25 @@ class Compiler {
       return;
     }
     if (a.cat == Ty::Mat || b.cat == Ty::Mat) mismatch();
+    if (shift) {
+      // e1 << e2, e1 >> e2: e1 an i32 / u32 scalar or vector, e2 u32 of the
+      // same shape; the low 5 bits of e2 are the amount (wgsl_rt.cuh shl)
+      if (!(is_int(a.s) && (b.s == SK::U32 || b.s == SK::AInt)) || a.cat != b.cat ||
+          (a.cat == Ty::Vec && a.n != b.n))
+        mismatch();
+      const bool folded = a.s == SK::AInt && L.cst && R.cst && a.cat == Ty::Scalar;
+      e.ty = a.cat == Ty::Vec ? vecT(concrete_sk(a.s), a.n) : scalar(folded ? SK::AInt : concrete_sk(a.s));
+      bi.tl = e.ty;
+      bi.tr = a.cat == Ty::Vec ? vecT(SK::U32, a.n) : scalar(SK::U32);
+      if (folded) {
+        e.cst = true;
+        long long x = (long long)L.cv, y = (long long)R.cv;
+        if (y < 0 || y >= 32) fail(e.line, e.col, "shift amount out of range in a constant expression");
+        e.cv = double(op == "<<" ? (x << y) : (x >> y));
+      }
+      bininfo[&e] = bi;
+      return;
+    }
     SK u;
     if (!unify_sk(a.s, b.s, u)) mismatch();
     int n = 1;
@@ -1605,16 +1624,6 @@ class Compiler {
         e.cst = true;
         long long x = (long long)L.cv, y = (long long)R.cv;
         e.cv = double(op == "&" ? (x & y) : op == "|" ? (x | y) : (x ^ y));
-      }
-    } else if (shift) {
-      if (!is_int(a.s) || !is_int(b.s)) mismatch();
-      e.ty = a.cat == Ty::Vec ? vecT(concrete_sk(a.s), n) : scalar(a.s == SK::AInt && L.cst && R.cst ? SK::AInt : concrete_sk(a.s));
-      bi.tl = e.ty;
-      bi.tr = b.cat == Ty::Vec ? vecT(SK::U32, n) : scalar(SK::U32);
-      if (L.cst && R.cst && e.ty.s == SK::AInt) {
-        e.cst = true;
-        long long x = (long long)L.cv, y = (long long)R.cv;
-        e.cv = double(op == "<<" ? (x << y) : (x >> y));
       }
     } else {
       mismatch();
@@ -2413,6 +2422,11 @@ class Compiler {
         const std::string& op = e.op;
         bool vec = e.args[0]->ty.cat == Ty::Vec || e.args[1]->ty.cat == Ty::Vec;
         if (op == "%" && is_float(e.ty.s)) return "::wgsl::fmod_wgsl(" + a + ", " + b + ")";
+        // integer '/' and '%' with WGSL's results for a zero divisor and for
+        // the most negative i32 over -1; shifts use the amount's low 5 bits
+        if ((op == "/" || op == "%") && (e.ty.s == SK::I32 || e.ty.s == SK::U32))
+          return std::string("::wgsl::") + (op == "/" ? "div_int(" : "mod_int(") + a + ", " + b + ")";
+        if (op == "<<" || op == ">>") return std::string("::wgsl::") + (op == "<<" ? "shl(" : "shr(") + a + ", " + b + ")";
         // dot(a, b) + s or s + dot(a, b) in f32: fast modules fold s into the
         // dot product's first FMA (wgsl_rt.cuh dot_add); precise modules and
         // the host add as written (IEEE addition commutes, so either order is

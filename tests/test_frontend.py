@@ -1014,3 +1014,78 @@ def test_const_assert_and_directive_diagnostics(helpers, body, needle):
     with pytest.raises(_abi.LinonCompileError) as e:
         translate_wgsl(body, helpers or None)
     assert needle in e.value.message, e.value.message
+
+
+def test_integer_division_modulo_and_shifts():
+    """WGSL's integer '/' and '%' (a / 0 = a, a % 0 = 0, most negative i32
+    over -1), shifts by the amount's low 5 bits (also vectors, i32 << u32),
+    and '%' with a vector and a scalar (integer and float)."""
+    rng = np.random.default_rng(41)
+    n = 2000
+    x = np.zeros((n, 13), np.float32)
+    ai = rng.integers(-2 ** 31, 2 ** 31, n, dtype=np.int64)
+    bi = rng.integers(-9, 10, n, dtype=np.int64)
+    ai[:6] = [-2 ** 31, -2 ** 31, 7, -7, 0, 2 ** 31 - 1]
+    bi[:6] = [-1, 0, 0, 0, 0, -1]
+    sh = rng.integers(0, 70, n, dtype=np.int64)
+    x[:, 3] = ai.astype(np.int32).view(np.float32)
+    x[:, 4] = bi.astype(np.int32).view(np.float32)
+    x[:, 5] = sh.astype(np.uint32).view(np.float32)
+    x[:, 9:12] = rng.uniform(-5, 5, (n, 3)).astype(np.float32)
+    body = """
+let a = bitcast<i32>(p.x);
+let b = bitcast<i32>(p.y);
+let s = bitcast<u32>(p.z);
+let ua = bitcast<u32>(a);
+let ub = bitcast<u32>(b);
+let va = vec2<i32>(a, b) / vec2<i32>(b, 3) + vec2<i32>(a, 7) % b;
+let q = a / b ^ (a % b) * 3;
+return bitcast<vec3<f32>>(vec3<u32>(bitcast<u32>(q) ^ (ua / ub) ^ ((ua % ub) << 7u),
+                                    bitcast<u32>(a << s) ^ bitcast<u32>(a >> s) ^ (ua >> s),
+                                    bitcast<u32>(va.x ^ va.y) ^ bitcast<u32>((vec2<i32>(a) << vec2<u32>(s, 1u)).x)));
+"""
+    out = _host_eval(body, x).view(np.uint32)
+
+    def s32(v):
+        v &= M32
+        return v - (1 << 32) if v & 0x80000000 else v
+
+    def div(a, b):
+        if b == 0 or (a == -2 ** 31 and b == -1):
+            return a
+        q = abs(a) // abs(b)
+        return q if (a >= 0) == (b > 0) else -q
+
+    def mod(a, b):
+        if b == 0 or (a == -2 ** 31 and b == -1):
+            return 0
+        return a - div(a, b) * b
+
+    def udiv(a, b):
+        return a if b == 0 else a // b
+
+    def umod(a, b):
+        return 0 if b == 0 else a % b
+
+    for k in range(n):
+        a, b, s = int(ai[k]), int(bi[k]), int(sh[k]) & 31
+        ua, ub = a & M32, b & M32
+        q = s32(div(a, b) ^ (mod(a, b) * 3))
+        e0 = (q & M32) ^ udiv(ua, ub) ^ ((umod(ua, ub) << 7) & M32)
+        e1 = ((ua << s) & M32) ^ ((a >> s) & M32) ^ (ua >> s)
+        va0 = s32(div(a, b) + mod(a, b))
+        va1 = s32(div(b, 3) + mod(7, b))
+        e2 = ((va0 ^ va1) & M32) ^ ((ua << s) & M32)
+        assert list(out[k]) == [e0 & M32, e1 & M32, e2 & M32], k
+    fb = "return vec3<f32>((v % 2.0).x, (3.0 % v).y, f32((vec3<i32>(7, -7, 9) % 4).y + (11 / vec2<i32>(2, 0)).y));"
+    out = _host_eval(fb, x)
+    v = x[:, 9:12]
+    want = np.stack([v[:, 0] - np.float32(2.0) * np.trunc(v[:, 0] / np.float32(2.0)),
+                     np.float32(3.0) - v[:, 1] * np.trunc(np.float32(3.0) / v[:, 1]),
+                     np.full(n, -3.0 + 11.0, np.float32)], -1).astype(np.float32)
+    np.testing.assert_array_equal(out, want)
+    with pytest.raises(_abi.LinonCompileError) as e:
+        translate_wgsl("let a = 1 << 40; return p;")
+    assert "shift amount out of range" in e.value.message
+    with pytest.raises(_abi.LinonCompileError):
+        translate_wgsl("let a = 1u << 2i; return p;")  # the amount must be u32
