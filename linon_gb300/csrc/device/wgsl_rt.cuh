@@ -334,6 +334,10 @@ WG_VEC_BINOP(+)
 WG_VEC_BINOP(-)
 WG_VEC_BINOP(*)
 WG_VEC_BINOP(/)
+// bitwise operators of integer vectors (bool vectors use land / lor)
+WG_VEC_BINOP(&)
+WG_VEC_BINOP(|)
+WG_VEC_BINOP(^)
 #undef WG_VEC_BINOP
 
 #if !defined(LINON_PRECISE) && defined(__CUDA_ARCH__)
@@ -349,6 +353,11 @@ template <int N> WG_HD vec<float, N> operator/(const vec<float, N>& a, float s) 
 template <class T, int N> WG_HD vec<T, N> operator-(const vec<T, N>& a) {
   vec<T, N> r;
   for (int i = 0; i < N; ++i) r[i] = -a[i];
+  return r;
+}
+template <class T, int N> WG_HD vec<T, N> operator~(const vec<T, N>& a) {  // integer vectors
+  vec<T, N> r;
+  for (int i = 0; i < N; ++i) r[i] = ~a[i];
   return r;
 }
 template <int N> WG_HD vec<bool, N> operator!(const vec<bool, N>& a) {

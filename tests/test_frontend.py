@@ -1089,3 +1089,14 @@ return bitcast<vec3<f32>>(vec3<u32>(bitcast<u32>(q) ^ (ua / ub) ^ ((ua % ub) << 
     assert "shift amount out of range" in e.value.message
     with pytest.raises(_abi.LinonCompileError):
         translate_wgsl("let a = 1u << 2i; return p;")  # the amount must be u32
+
+
+def test_vector_complement_and_bitwise_ops():
+    x, raw = _bits_inputs(200)
+    body = """let u = bitcast<vec3<u32>>(p);
+let i = bitcast<vec3<i32>>(p);
+return bitcast<vec3<f32>>((~u) ^ bitcast<vec3<u32>>(~i & i) ^ (u | vec3<u32>(1u)));"""
+    out = _host_eval(body, x).view(np.uint32)
+    u = raw.astype(np.int64)
+    want = ((~u) & M32) ^ 0 ^ (u | 1)
+    np.testing.assert_array_equal(out, want.astype(np.uint32))
