@@ -1618,7 +1618,8 @@ class Compiler {
         // fold only to keep abstract operands out of C++; result stays a bool expression
       }
     } else if (bits) {
-      if (!(is_int(u) || u == SK::Bool)) mismatch();
+      // & | ^ on integers; & | also on bools (WGSL has no bool ^)
+      if (!(is_int(u) || (u == SK::Bool && op != "^"))) mismatch();
       e.ty = cat == Ty::Vec ? vecT(u, n) : scalar(u);
       if (L.cst && R.cst && cat == Ty::Scalar && u == SK::AInt) {
         e.cst = true;

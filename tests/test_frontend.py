@@ -1100,3 +1100,63 @@ return bitcast<vec3<f32>>((~u) ^ bitcast<vec3<u32>>(~i & i) ^ (u | vec3<u32>(1u)
     u = raw.astype(np.int64)
     want = ((~u) & M32) ^ 0 ^ (u | 1)
     np.testing.assert_array_equal(out, want.astype(np.uint32))
+
+
+def test_every_accepted_operator_combination_compiles():
+    """Each binary operator over every pair of scalar / vec2 operand types
+    (f32, i32, u32, bool), and each unary operator: the front end accepts
+    exactly the combinations WGSL defines, and everything it accepts
+    compiles (host g++ and NVRTC for sm_103a)."""
+    types = ["f32", "i32", "u32", "bool", "vec2<f32>", "vec2<i32>", "vec2<u32>", "vec2<bool>"]
+    binops = ["+", "-", "*", "/", "%", "&", "|", "^", "<<", ">>", "<", "<=", ">", ">=", "==", "!=", "&&", "||"]
+    num = {"f32", "i32", "u32"}
+
+    def kind(t):
+        return t.replace("vec2<", "").replace(">", "")
+
+    def wgsl_defines(a, b, op):
+        ka, kb, va, vb = kind(a), kind(b), a.startswith("vec"), b.startswith("vec")
+        if op in ("+", "-", "*", "/", "%"):
+            return ka == kb and ka in num                       # scalar/vector mixes allowed
+        if op in ("<", "<=", ">", ">="):
+            return ka == kb and ka in num and va == vb
+        if op in ("==", "!="):
+            return ka == kb and va == vb
+        if op in ("&", "|"):
+            return ka == kb and va == vb and ka in ("i32", "u32", "bool")
+        if op == "^":
+            return ka == kb and va == vb and ka in ("i32", "u32")
+        if op in ("<<", ">>"):
+            return ka in ("i32", "u32") and kb == "u32" and va == vb
+        return ka == kb == "bool" and not va and not vb           # && ||
+
+    lines = []
+    for a in types:
+        for b in types:
+            for op in binops:
+                stmt = f"{{ let x = {a}(); let y = {b}(); let z{len(lines)} = x {op} y; }}"
+                try:
+                    translate_wgsl(stmt + "\nreturn p;")
+                    ok = True
+                except _abi.LinonCompileError:
+                    ok = False
+                assert ok == wgsl_defines(a, b, op), (a, op, b, ok)
+                if ok:
+                    lines.append(stmt)
+    for a in types:
+        for op in ["-", "!", "~"]:
+            stmt = f"{{ let x = {a}(); let z = {op}x; }}"
+            try:
+                translate_wgsl(stmt + "\nreturn p;")
+                ok = True
+            except _abi.LinonCompileError:
+                ok = False
+            k = kind(a)
+            assert ok == ((op == "-" and k in ("f32", "i32")) or (op == "!" and k == "bool")
+                          or (op == "~" and k in ("i32", "u32"))), (op, a, ok)
+            if ok:
+                lines.append(stmt)
+    assert len(lines) == 136
+    body = "\n".join(lines) + "\nreturn p;"
+    _host_eval(body, np.zeros((2, 13), np.float32))           # compiles for the host
+    assert "linon_march_v14" in validate_field(body)          # and for the GPU
