@@ -646,8 +646,17 @@ template <int N> WG_HD float dot_add(const vec<float, N>& a, const vec<float, N>
   return r;
 #endif
 }
-WG_HD int dot(const vec2i& a, const vec2i& b) { return a.x * b.x + a.y * b.y; }
-WG_HD int dot(const vec3i& a, const vec3i& b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+// integer dot products wrap like WGSL's i32 / u32 arithmetic (summed in u32)
+template <int N> WG_HD int dot(const vec<int, N>& a, const vec<int, N>& b) {
+  unsigned r = 0u;
+  for (int i = 0; i < N; ++i) r += unsigned(a[i]) * unsigned(b[i]);
+  return int(r);
+}
+template <int N> WG_HD unsigned dot(const vec<unsigned, N>& a, const vec<unsigned, N>& b) {
+  unsigned r = 0u;
+  for (int i = 0; i < N; ++i) r += a[i] * b[i];
+  return r;
+}
 WG_HD vec3f cross(const vec3f& a, const vec3f& b) {
   return vec3f(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }

@@ -1160,3 +1160,35 @@ def test_every_accepted_operator_combination_compiles():
     body = "\n".join(lines) + "\nreturn p;"
     _host_eval(body, np.zeros((2, 13), np.float32))           # compiles for the host
     assert "linon_march_v14" in validate_field(body)          # and for the GPU
+
+
+def test_every_accepted_builtin_call_compiles():
+    """The numeric builtins called with one to three arguments of each
+    scalar / vector type (and the extra shapes of extractBits, insertBits,
+    ldexp, select, mix): every call the front end accepts compiles for the
+    host and for sm_103a."""
+    names = ("abs acos acosh asin asinh atan atanh atan2 ceil clamp cos cosh countLeadingZeros countOneBits "
+             "countTrailingZeros cross degrees determinant distance dot exp exp2 extractBits faceForward "
+             "firstLeadingBit firstTrailingBit floor fma fract frexp insertBits inverseSqrt ldexp length log log2 "
+             "max min mix modf normalize pow quantizeToF16 radians reflect refract reverseBits round saturate sign "
+             "sin sinh smoothstep sqrt step tan tanh transpose trunc select all any").split()
+    types = [f"{v}{k}" for v in ("", "vec2<", "vec3<", "vec4<") for k in ("f32", "i32", "u32", "bool")]
+    types = [t + (">" if t.startswith("vec") else "") for t in types]
+    lines = []
+    for n in names:
+        for t in types:
+            for args in (f"{t}()", f"{t}(), {t}()", f"{t}(), {t}(), {t}()", f"{t}(), 1u, 2u",
+                         f"{t}(), {t}(), 1u, 2u", f"{t}(), 2", f"{t}(), {t}(), true", f"{t}(), {t}(), 0.5"):
+                stmt = f"{{ let z{len(lines)} = {n}({args}); }}"
+                try:
+                    translate_wgsl(stmt + "\nreturn p;")
+                except _abi.LinonCompileError:
+                    continue
+                lines.append(stmt)
+    assert len(lines) > 250, len(lines)
+    body = "\n".join(lines) + "\nreturn p;"
+    _host_eval(body, np.zeros((2, 13), np.float32))
+    assert "linon_march_v14" in validate_field(body)
+    v = _host_eval("return vec3<f32>(f32(dot(vec4<i32>(1, -2, 3, 4), vec4<i32>(5, 6, -7, 8))),"
+                   " f32(dot(vec2<u32>(3u, 4u), vec2<u32>(5u, 6u))), 0.0);", np.zeros((1, 13), np.float32))
+    np.testing.assert_array_equal(v[0], [5 - 12 - 21 + 32, 39, 0])
