@@ -551,6 +551,33 @@ template <int N> WG_HD vec<float, N> fmod_wgsl(float a, const vec<float, N>& b) 
   return r;
 }
 
+// i32 + - * and unary - wrap on overflow (WGSL 8.7), computed in u32
+WG_HD int add_i32(int a, int b) { return int(unsigned(a) + unsigned(b)); }
+WG_HD int sub_i32(int a, int b) { return int(unsigned(a) - unsigned(b)); }
+WG_HD int mul_i32(int a, int b) { return int(unsigned(a) * unsigned(b)); }
+WG_HD int neg_i32(int a) { return int(0u - unsigned(a)); }
+#define WG_I32_BINARY(NAME)                                                            \
+  template <int N> WG_HD vec<int, N> NAME(const vec<int, N>& a, const vec<int, N>& b) { \
+    vec<int, N> r;                                                                     \
+    for (int i = 0; i < N; ++i) r[i] = NAME(a[i], b[i]);                               \
+    return r;                                                                          \
+  }                                                                                    \
+  template <int N> WG_HD vec<int, N> NAME(const vec<int, N>& a, int b) {               \
+    return NAME(a, vec<int, N>(b));                                                    \
+  }                                                                                    \
+  template <int N> WG_HD vec<int, N> NAME(int a, const vec<int, N>& b) {               \
+    return NAME(vec<int, N>(a), b);                                                    \
+  }
+WG_I32_BINARY(add_i32)
+WG_I32_BINARY(sub_i32)
+WG_I32_BINARY(mul_i32)
+#undef WG_I32_BINARY
+template <int N> WG_HD vec<int, N> neg_i32(const vec<int, N>& a) {
+  vec<int, N> r;
+  for (int i = 0; i < N; ++i) r[i] = neg_i32(a[i]);
+  return r;
+}
+
 // Integer division and remainder (WGSL 8.7): a / 0 = a, a % 0 = 0, and for
 // i32 the most negative value over -1 gives itself / 0 (no trap, no
 // undefined behaviour); otherwise truncating.

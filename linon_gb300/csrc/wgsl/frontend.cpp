@@ -2415,6 +2415,7 @@ class Compiler {
         if (e.cst) return lit_as(e.cv, concretize(e.ty), e.line, e.col);
         // a pointer is a C++ reference: &x and *p are the reference itself
         if (e.op == "&" || e.op == "*") return ex(*e.args[0]);
+        if (e.op == "-" && e.ty.s == SK::I32) return "::wgsl::neg_i32(" + ex(*e.args[0]) + ")";  // -INT_MIN wraps
         return "(" + e.op + ex(*e.args[0]) + ")";
       case Expr::Binary: {
         if (e.cst) return lit_as(e.cv, concretize(e.ty), e.line, e.col);
@@ -2428,6 +2429,10 @@ class Compiler {
         if ((op == "/" || op == "%") && (e.ty.s == SK::I32 || e.ty.s == SK::U32))
           return std::string("::wgsl::") + (op == "/" ? "div_int(" : "mod_int(") + a + ", " + b + ")";
         if (op == "<<" || op == ">>") return std::string("::wgsl::") + (op == "<<" ? "shl(" : "shr(") + a + ", " + b + ")";
+        // i32 + - * wrap on overflow (WGSL); computed in u32, no undefined behaviour
+        if ((op == "+" || op == "-" || op == "*") && e.ty.s == SK::I32)
+          return std::string("::wgsl::") + (op == "+" ? "add_i32(" : op == "-" ? "sub_i32(" : "mul_i32(") + a + ", " +
+                 b + ")";
         // dot(a, b) + s or s + dot(a, b) in f32: fast modules fold s into the
         // dot product's first FMA (wgsl_rt.cuh dot_add); precise modules and
         // the host add as written (IEEE addition commutes, so either order is

@@ -1192,3 +1192,20 @@ def test_every_accepted_builtin_call_compiles():
     v = _host_eval("return vec3<f32>(f32(dot(vec4<i32>(1, -2, 3, 4), vec4<i32>(5, 6, -7, 8))),"
                    " f32(dot(vec2<u32>(3u, 4u), vec2<u32>(5u, 6u))), 0.0);", np.zeros((1, 13), np.float32))
     np.testing.assert_array_equal(v[0], [5 - 12 - 21 + 32, 39, 0])
+
+
+def test_i32_arithmetic_wraps():
+    """i32 + - * and unary - wrap on overflow, as WGSL defines (the generated
+    code computes them in u32: no undefined behaviour on the host or GPU)."""
+    x = np.zeros((1, 13), np.float32)
+    x[0, 3:6] = np.array([2 ** 31 - 1, -2 ** 31, 65536], np.int32).view(np.float32)
+    body = """let m = bitcast<i32>(p.x);
+let n = bitcast<i32>(p.y);
+let k = bitcast<i32>(p.z);
+let v = vec2<i32>(m, n) + vec2<i32>(1, -1);
+return bitcast<vec3<f32>>(vec3<i32>(m + 1, (-n) ^ (k * k), v.x ^ v.y ^ (n - 1) ^ (vec2<i32>(k) * k).y));"""
+    out = _host_eval(body, x).view(np.int32)[0]
+    i32min = -2 ** 31
+    assert out[0] == i32min                                   # INT_MAX + 1
+    assert out[1] == (i32min ^ 0)                             # -INT_MIN = INT_MIN; 65536 * 65536 = 0
+    assert out[2] == (i32min ^ (2 ** 31 - 1) ^ (2 ** 31 - 1) ^ 0)
