@@ -1209,3 +1209,58 @@ return bitcast<vec3<f32>>(vec3<i32>(m + 1, (-n) ^ (k * k), v.x ^ v.y ^ (n - 1) ^
     assert out[0] == i32min                                   # INT_MAX + 1
     assert out[1] == (i32min ^ 0)                             # -INT_MIN = INT_MIN; 65536 * 65536 = 0
     assert out[2] == (i32min ^ (2 ** 31 - 1) ^ (2 ** 31 - 1) ^ 0)
+
+
+def test_fuzzed_fields_never_crash_and_compile_when_accepted():
+    """Seeded token mutations of the predefined fields and of this file's
+    test bodies: the front end returns a status for every one (no crash, no
+    hang), and every mutant it accepts compiles for the host."""
+    import random
+    import re as _re
+    rng = random.Random(2024)
+    lib = _abi.load()
+    pool = [(predefined_source(i), None) for i in range(1, 15)]
+    pool += [(POINTER_BODY, POINTER_HELPERS), (NESTED_BODY, NESTED_HELPERS),
+             (ALIAS_OVERRIDE_BODY, ALIAS_OVERRIDE_HELPERS), (ALL_NEW_BUILTINS_BODY, None),
+             (SWITCH_BODY, None), (STRUCT_BODY, STRUCT_HELPERS)]
+    toks = ["(", ")", ";", ",", ".", "&", "*", "-", "!", "~", "+", "%", "/", "<<", ">>", "^", "|", "&&", "==", "<",
+            "let", "var", "1", "1.5", "2u", "-3", "p", "v", "t", "x", "i32", "f32", "u32", "vec2", "vec3<i32>",
+            "vec3<u32>", "select", "abs", "max", "dot", "countOneBits", "frexp", "[0]", ".xy", "true"]
+    out = C.create_string_buffer(1 << 20)
+    log = C.create_string_buffer(1 << 16)
+    accepted = {}
+    for _ in range(2500):
+        body, helpers = rng.choice(pool)
+        mut_helpers = helpers is not None and rng.random() < 0.5
+        words = _re.findall(r"\w+|[^\w\s]+|\s+", helpers if mut_helpers else body)
+        for _k in range(rng.randint(1, 3)):
+            i = rng.randrange(len(words))
+            r = rng.random()
+            if r < 0.35:
+                del words[i]
+            elif r < 0.7:
+                words.insert(i, rng.choice(toks))
+            else:
+                words[i] = rng.choice(toks)
+        m = "".join(words)
+        b, h = (body, m) if mut_helpers else (m, helpers)
+        st = lib.linon_wgsl_translate(b.encode(), h.encode() if h else None, out, len(out), log, len(log))
+        assert st in (_abi.LINON_OK, _abi.LINON_ECOMPILE)
+        if st == _abi.LINON_OK:
+            accepted[out.value] = True
+    assert len(accepted) > 50
+    d = Path(tempfile.mkdtemp(prefix="linon_fuzz_"))
+    files = []
+    for k, code in enumerate(accepted):
+        f = d / f"m{k}.cpp"
+        f.write_text(f'#include "{RT}"\n' + code.decode())
+        files.append(f)
+    failures = []
+    for k in range(0, len(files), 32):
+        procs = [(f, subprocess.Popen(["g++", "-std=c++17", "-fsyntax-only", str(f)], stderr=subprocess.PIPE,
+                                      text=True)) for f in files[k:k + 32]]
+        for f, p in procs:
+            _, err = p.communicate(timeout=120)
+            if p.returncode != 0:
+                failures.append((f.read_text()[-600:], err[:600]))
+    assert not failures, failures[:2]
