@@ -527,7 +527,11 @@ class Parser {
         expect("=");
         type();  // checked here; uses re-read it from aliases_
         expect(";");
-      } else if (is_kw("var") || is_kw("enable")) {
+      } else if (is_kw("enable")) {
+        fail(cur().line, cur().col,
+             "'enable' extensions are not available: the reference's device requests no optional WGSL "
+             "feature (f16 needs SHADER_F16)");
+      } else if (is_kw("var")) {
         fail(cur().line, cur().col, "'" + cur().s + "' declarations are not supported in field function modules");
       } else if (cur().t == TT::Punct && cur().s == ";") {
         next();

@@ -1009,6 +1009,7 @@ const_assert 1.5 < 2.0;
     ("", "const_assert 1; return p;", "needs a bool expression"),
     ("requires no_such_extension;", "return p;", "unknown language extension"),
     ("diagnostic(loud, derivative_uniformity);", "return p;", "unknown diagnostic severity"),
+    ("enable f16;", "return p;", "SHADER_F16"),
 ])
 def test_const_assert_and_directive_diagnostics(helpers, body, needle):
     with pytest.raises(_abi.LinonCompileError) as e:
