@@ -25,6 +25,27 @@ def test_request_stream_is_seeded_and_mixed():
     assert caps[0].pos.shape == (256, 2) and caps[0].req.n_steps == 3999
 
 
+def test_summarize_statistics():
+    """Serving summary on synthetic records: failed requests excluded,
+    percentiles per kind, throughput over the span of completed requests."""
+    recs = []
+    for i in range(100):
+        recs.append({"status": 0, "latency_ms": float(i + 1), "t_submit_ms": float(i), "t_done_ms": float(i + 10),
+                     "label": "frame" if i % 4 else "capture", "ray_steps": 1000, "wave": i // 10})
+    recs.append({"status": 4, "latency_ms": 1e9, "t_submit_ms": 0.0, "t_done_ms": 1e9, "label": "frame",
+                 "ray_steps": 10 ** 12, "wave": 99})
+    sm = serving.summarize(recs)
+    assert sm["requests"] == 101 and sm["completed"] == 100
+    assert sm["p50_ms"] == np.percentile(np.arange(1, 101), 50) and sm["max_ms"] == 100.0
+    assert sm["p99_ms"] == np.percentile(np.arange(1, 101), 99)
+    assert sm["waves"] == 10
+    assert abs(sm["span_s"] - 0.109) < 1e-12                       # first submit 0 ms, last done 109 ms
+    assert abs(sm["ray_steps_per_s"] - 100 * 1000 / 0.109) < 1e-6
+    assert sm["by_kind"]["capture"]["n"] == 25 and sm["by_kind"]["frame"]["n"] == 75
+    lat_c = [float(i + 1) for i in range(100) if i % 4 == 0]
+    assert sm["by_kind"]["capture"]["p50_ms"] == np.percentile(lat_c, 50)
+
+
 def _setup(engine, precise=False):
     xyz, faces, rgb = scene.cornell_with_spheres(seed=2, subdivisions=3)
     engine.upload_scene(xyz, faces, rgb, bvh=True)
