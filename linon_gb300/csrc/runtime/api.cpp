@@ -185,9 +185,11 @@ std::string module_source(const std::string& field_cuda, const std::vector<int>&
   // frames 63.6 -> 62.9 ms), slower in the batched ones (not defined there)
   s << "#define LINON_PACKED_NORMALIZE 1\n#include \"march.cuh\"\n" << field_cuda << R"LINON(
 struct LinonField {
+  // the ray's var<private> state: one functor per thread and ray
+  mutable linon_user::Private pv;
   __device__ __forceinline__ wgsl::vec3f operator()(const wgsl::vec3f& pp, const wgsl::vec3f& p,
       const wgsl::vec3f& v0, const wgsl::vec3f& v, float t) const {
-    return linon_user::field_function(pp, p, v0, v, t);
+    return linon_user::field_function(pv, pp, p, v0, v, t);
   }
 };
 )LINON";
@@ -621,6 +623,7 @@ int linon_field_compile(linon_ctx* ctx, const char* field_body, const char* help
   f->body = field_body;
   f->helpers = helpers_src ? helpers_src : "";
   f->cuda = t.code;
+  f->stateful = t.has_private;
   f->flags = flags;
   f->flops_arith = t.flops_arith;
   f->flops_transc = t.flops_transc;

@@ -48,9 +48,10 @@ std::string batch_module_source(const std::vector<const linon_field*>& fields) {
   // (the one-CTA-per-tile kernels, whose CTAs lie in one view)
   for (size_t i = 0; i < fields.size(); ++i)
     s << "struct LinonField" << i << " {\n"
+         "  mutable linon_user_" << i << "::Private pv;\n"
          "  __device__ __forceinline__ wgsl::vec3f operator()(const wgsl::vec3f& pp, const wgsl::vec3f& p,\n"
          "      const wgsl::vec3f& v0, const wgsl::vec3f& v, float t) const {\n"
-         "    return linon_user_" << i << "::field_function(pp, p, v0, v, t);\n  }\n};\n";
+         "    return linon_user_" << i << "::field_function(pv, pp, p, v0, v, t);\n  }\n};\n";
   s << "struct LinonFields {\n"
        "  __device__ __forceinline__ wgsl::vec3f operator()(int i, const wgsl::vec3f& pp, const wgsl::vec3f& p,\n"
        "      const wgsl::vec3f& v0, const wgsl::vec3f& v, float t) const {\n"
@@ -175,6 +176,15 @@ int validate_batch(const linon_ctx* ctx, const linon_field* const* fields, int32
 // fields, for compile checks without a context.
 std::string batched_module_source(const std::vector<const linon_field*>& fields) {
   return batch_module_source(fields);
+}
+
+// Fields with var<private> state need one field functor per ray for the
+// whole march: the one-CTA-per-tile schedule has it, the persistent queue
+// (a functor per quantum, or per evaluation in a mixed warp) does not.
+bool any_stateful(const linon_field* const* fields, int n_fields) {
+  for (int i = 0; i < n_fields; ++i)
+    if (fields[i] && fields[i]->stateful) return true;
+  return false;
 }
 
 int batch_tuning(const linon_ctx* ctx, const linon_batch_tuning* in, linon_batch_tuning& t) {
@@ -335,6 +345,7 @@ int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields, int32_t
     if (int st = get_module(ctx, bs, fields, n_fields, mod)) return st;
     linon_batch_tuning t;
     if (int st = batch_tuning(ctx, tuning, t)) return st;
+    if (any_stateful(fields, n_fields)) t.schedule = 2;
     std::vector<BatchView> tab;
     int n_blocks = 0;
     const long long begin = batch_table(views, n_views, t, tab, &n_blocks);
@@ -432,10 +443,12 @@ int linon_autotune_batch(linon_ctx* ctx, const linon_field* const* fields, int32
   cudaEventCreate(&e1);
   double best_t = 1e300;
   linon_batch_tuning bt{};
+  const bool stateful = any_stateful(fields, n_fields);
   for (int q : quanta)
     for (int b : blocks)
       for (auto& tl : tiles)
         for (int rf : refills) {
+        if (stateful) continue;  // persistent queue: not for fields with var<private> state
         linon_batch_tuning t{};
         t.schedule = 1;
         t.quantum = q;

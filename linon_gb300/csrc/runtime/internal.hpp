@@ -66,6 +66,7 @@ int jit_compile(const std::string& source, bool precise, const std::vector<std::
 // log carries the compiler's and ptxas' messages (registers, spills).
 int jit_check(const std::string& source, bool precise, std::string& log, size_t* cubin_bytes);
 std::string batched_module_source(const std::vector<const linon_field*>& fields);
+bool any_stateful(const linon_field* const* fields, int n_fields);
 
 // ---- BVH ----------------------------------------------------------------
 struct BvhBuild {
@@ -107,6 +108,7 @@ struct linon_field {
   std::string body, helpers, cuda;
   int flags = 0;
   int flops_arith = 0, flops_transc = 0;
+  bool stateful = false;  // var<private> state: batches use the one-CTA-per-tile schedule
   std::shared_ptr<linon::JitModule> mod;  // capture, field_eval, base march variant
   mutable std::mutex vmu;                  // guards `variants`
   mutable std::map<int, std::shared_ptr<linon::JitModule>> variants;  // other march variants

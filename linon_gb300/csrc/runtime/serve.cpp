@@ -392,6 +392,7 @@ int linon_serve_start(linon_ctx* ctx, const linon_field* const* fields, int32_t 
     if (s->cfg.slots > 8) s->cfg.slots = 8;
     if (s->cfg.max_wave <= 0) s->cfg.max_wave = 256;
     if (int st = batch_tuning(ctx, &s->cfg.tuning, s->tuning)) return st;
+    if (any_stateful(fields, n_fields)) s->tuning.schedule = 2;
     if (int st = batch_module(ctx, fields, n_fields, s->mod)) return st;
     // keep freed pool memory cached (no release to the OS between waves)
     cudaMemPool_t pool;

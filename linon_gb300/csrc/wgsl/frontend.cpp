@@ -424,6 +424,7 @@ struct GConst {
   int line = 0, col = 0;
   bool is_override = false;  // `override`: the default value, a concrete scalar
   bool is_assert = false;    // module-scope const_assert (no name, no value)
+  bool is_private = false;   // var<private>: per-invocation state (a member of Private)
   bool has_ty = false;
   Ty ty;
   EP e;
@@ -531,6 +532,26 @@ class Parser {
         fail(cur().line, cur().col,
              "'enable' extensions are not available: the reference's device requests no optional WGSL "
              "feature (f16 needs SHADER_F16)");
+      } else if (is_kw("var") && peek().t == TT::Punct && peek().s == "<") {
+        // var<private> name[: T][ = init];  state of one invocation (one ray)
+        Tok k = next();
+        expect("<");
+        Tok sp = cur();
+        const std::string space = ident("address space");
+        if (space != "private")
+          fail(sp.line, sp.col, "only var<private> is allowed at module scope in a field function module, found '" +
+                                    space + "'");
+        close_template();
+        auto g = std::make_unique<GConst>();
+        g->line = k.line;
+        g->col = k.col;
+        g->is_private = true;
+        g->name = ident("variable name");
+        if (accept(":")) { g->has_ty = true; g->ty = type(); }
+        if (accept("=")) g->e = expr();
+        else if (!g->has_ty) fail(k.line, k.col, "'var<private>' needs a type or an initializer");
+        expect(";");
+        consts.push_back(std::move(g));
       } else if (is_kw("var")) {
         fail(cur().line, cur().col, "'" + cur().s + "' declarations are not supported in field function modules");
       } else if (cur().t == TT::Punct && cur().s == ";") {
@@ -1203,6 +1224,8 @@ class Compiler {
   std::vector<std::map<std::string, Sym>> scopes;
   Func* cur_fn = nullptr;
   std::vector<std::string> const_code;
+  std::vector<std::string> private_code;  // members of struct Private (var<private>)
+  bool in_module_init = false;  // checking a module constant or a private initializer
   int loop_depth = 0;
 
   static bool is_helper(const std::string& n) {
@@ -1325,6 +1348,37 @@ class Compiler {
     if (g.state == 2) return;
     if (g.state == 1) fail(g.line, g.col, "cyclic constant definition '" + g.name + "'");
     g.state = 1;
+    if (g.is_private) {
+      auto saved = scopes;
+      scopes.clear();
+      scopes.emplace_back();
+      Ty t;
+      std::string init;
+      if (g.e) {
+        const bool saved_init = in_module_init;
+        in_module_init = true;
+        check(*g.e);
+        in_module_init = saved_init;
+        if (g.e->ty.cat == Ty::Void) fail(g.line, g.col, "initializer has no value");
+        t = g.has_ty ? g.ty : concretize(g.e->ty);
+        if (g.has_ty && !(g.e->ty == t || ty_convertible(g.e->ty, t)))
+          fail(g.line, g.col, "cannot initialize '" + g.name + "' of type " + wgsl_name(t) + " with " + wgsl_name(g.e->ty));
+        init = ex_as(*g.e, t);
+      } else {
+        t = g.ty;
+        init = cpp_name(t) + "()";
+      }
+      if (t.cat == Ty::Ptr) fail(g.line, g.col, "a private variable cannot be a pointer");
+      scopes = saved;
+      private_code.push_back("  " + cpp_name(t) + " u_" + g.name + " = " + init + ";");
+      Sym sym;
+      sym.ty = t;
+      sym.is_var = true;
+      sym.cpp = "pv.u_" + g.name;
+      gsyms[g.name] = sym;
+      g.state = 2;
+      return;
+    }
     if (g.is_assert) {
       auto saved = scopes;
       scopes.clear();
@@ -1337,7 +1391,10 @@ class Compiler {
     auto saved = scopes;
     scopes.clear();
     scopes.emplace_back();
+    const bool saved_init = in_module_init;
+    in_module_init = true;
     check(*g.e);
+    in_module_init = saved_init;
     if (g.is_override) {
       // an override is a concrete scalar: its declared type, or its default
       // value's type made concrete
@@ -1429,6 +1486,8 @@ class Compiler {
       if (fmap.count(e.op) || is_helper(e.op)) fail(e.line, e.col, "function '" + e.op + "' used as a value");
       fail(e.line, e.col, "no definition in scope for identifier: '" + e.op + "'");
     }
+    if (in_module_init && s->cpp.compare(0, 3, "pv.") == 0)
+      fail(e.line, e.col, "'" + e.op + "' is a private variable: module initializers must be constant");
     e.ty = s->ty;
     e.cst = s->cst;
     e.cv = s->cv;
@@ -2524,7 +2583,10 @@ class Compiler {
             }
             return s + ")";
           }
-          default: return ci.fn + "(" + join(0) + ")";
+          default:
+            // user functions also receive the invocation's private variables
+            if (ci.fn.compare(0, 2, "u_") == 0) return ci.fn + "(pv" + (as.empty() ? "" : ", ") + join(0) + ")";
+            return ci.fn + "(" + join(0) + ")";
         }
       }
     }
@@ -2898,14 +2960,15 @@ class Compiler {
     loop_depth = 0;
     switch_depth = 0;
     cur_fn = &f;
-    std::string params;
+    // every function receives the invocation's private variables
+    std::string params = "Private& pv";
     for (size_t i = 0; i < f.params.size(); ++i) {
       const Param& p = f.params[i];
       Sym s;
       s.ty = p.ty;
       s.cpp = fresh(p.name);
       declare(p.name, s, p.line, p.col);
-      params += (i ? ", " : "") + cpp_name(p.ty) + " " + s.cpp;
+      params += ", " + cpp_name(p.ty) + " " + s.cpp;
     }
     std::string body;
     Cost c;
@@ -2999,6 +3062,10 @@ Translation translate(const std::string& field_body, const std::string& helpers_
       os << " {}\n};\n";
     }
     for (auto& c : cc.const_code) os << c << "\n";
+    // the state of one invocation (one ray): var<private> variables
+    os << "struct Private {\n";
+    for (auto& m : cc.private_code) os << m << "\n";
+    os << "};\n";
     // prototypes (WGSL functions may be used before their declaration)
     for (auto& f : cc.fns) {
       if (f->name == "field_function") continue;
@@ -3011,6 +3078,7 @@ Translation translate(const std::string& field_body, const std::string& helpers_
     tr.code = os.str();
     tr.flops_arith = field->fl;
     tr.flops_transc = field->tr;
+    tr.has_private = !cc.private_code.empty();
   } catch (const CompileError& e) {
     std::ostringstream os;
     os << "error: " << e.what() << "\n";

@@ -21,10 +21,14 @@ struct Translation {
   std::string log;       // diagnostics (errors) when !ok
   int flops_arith = 0;   // counted FP32 add/mul/div/sqrt of one evaluation
   int flops_transc = 0;  // transcendental calls of one evaluation
+  bool has_private = false;  // the module declares var<private> state
 };
 
 // ns: C++ namespace that receives the generated functions; the field is
-// ns::field_function(vec3f p_prev, vec3f p, vec3f v0, vec3f v, float t).
+// ns::field_function(ns::Private& pv, vec3f p_prev, vec3f p, vec3f v0,
+// vec3f v, float t), where ns::Private holds the module's var<private>
+// variables (an empty struct when there are none): one Private per
+// invocation, i.e. per ray.
 Translation translate(const std::string& field_body, const std::string& helpers_src,
                       const std::string& ns);
 

@@ -44,7 +44,7 @@ def host_fields(lib):
     parts.append("    wgsl::vec3f pp(q[0],q[1],q[2]), p(q[3],q[4],q[5]), v0(q[6],q[7],q[8]), v(q[9],q[10],q[11]);")
     parts.append("    switch (id) {")
     for fid in EVAL_IDS:
-        parts.append(f"      case {fid}: r = f{fid}::field_function(pp, p, v0, v, q[12]); break;")
+        parts.append(f"      case {fid}: {{ f{fid}::Private pv; r = f{fid}::field_function(pv, pp, p, v0, v, q[12]); }} break;")
     parts.append("      default: return 1; }")
     parts.append("    out[3*i] = r.x; out[3*i+1] = r.y; out[3*i+2] = r.z; }")
     parts.append("  return 0; }")
@@ -198,15 +198,18 @@ def test_validate_rejects_front_end_errors():
         validate_field("return undefined_thing;")
 
 
-def _host_eval(body, x, helpers=None):
+def _host_eval(body, x, helpers=None, calls=1):
     """Lowers one field body, compiles it for the host with g++ and
-    evaluates it on inputs [n, 13] (p_prev, p, v0, v, t)."""
+    evaluates it on inputs [n, 13] (p_prev, p, v0, v, t): one invocation per
+    input (fresh var<private> state), the field called `calls` times in it,
+    the last result returned."""
     code = translate_wgsl(body, helpers)
     src = "\n".join([f'#include "{RT}"', code,
-                     'extern "C" void eval(const float* in, long n, float* out) {',
+                     'extern "C" void eval(const float* in, long n, float* out, int calls) {',
                      "  for (long i = 0; i < n; ++i) { const float* q = in + 13 * i;",
                      "    wgsl::vec3f pp(q[0],q[1],q[2]), p(q[3],q[4],q[5]), v0(q[6],q[7],q[8]), v(q[9],q[10],q[11]);",
-                     "    wgsl::vec3f r = linon_user::field_function(pp, p, v0, v, q[12]);",
+                     "    linon_user::Private pv; wgsl::vec3f r;",
+                     "    for (int c = 0; c < calls; ++c) r = linon_user::field_function(pv, pp, p, v0, v, q[12]);",
                      "    out[3*i] = r.x; out[3*i+1] = r.y; out[3*i+2] = r.z; } }"])
     d = Path(tempfile.mkdtemp(prefix="linon_fe1_"))
     (d / "f.cpp").write_text(src)
@@ -214,10 +217,10 @@ def _host_eval(body, x, helpers=None):
                         str(d / "f.cpp")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     h = C.CDLL(str(d / "f.so"))
-    h.eval.argtypes = [C.c_void_p, C.c_long, C.c_void_p]
+    h.eval.argtypes = [C.c_void_p, C.c_long, C.c_void_p, C.c_int]
     x = np.ascontiguousarray(x, np.float32)
     out = np.zeros((len(x), 3), np.float32)
-    h.eval(x.ctypes.data, len(x), out.ctypes.data)
+    h.eval(x.ctypes.data, len(x), out.ctypes.data, int(calls))
     return out
 
 
@@ -1265,3 +1268,52 @@ def test_fuzzed_fields_never_crash_and_compile_when_accepted():
             if p.returncode != 0:
                 failures.append((f.read_text()[-600:], err[:600]))
     assert not failures, failures[:2]
+
+
+PRIVATE_HELPERS = """
+var<private> calls: u32 = 0u;
+var<private> acc: vec3<f32>;
+var<private> hist: array<f32, 4>;
+fn note(x: f32) {
+    hist[calls % 4u] = x;
+    acc += vec3<f32>(x, 1.0, 0.0);
+}
+"""
+PRIVATE_BODY = """
+calls += 1u;
+note(t * f32(calls));
+return acc + vec3<f32>(hist[0] + hist[1] + hist[2] + hist[3], f32(calls), 0.0);
+"""
+
+
+def test_private_variables_persist_within_an_invocation():
+    """var<private>: one state per invocation (one ray), initialised from
+    its initialiser or zero, kept across the field's calls in that
+    invocation, written by helper functions."""
+    x = np.zeros((3, 13), np.float32)
+    x[:, 12] = [1.0, 2.0, 0.5]
+    for calls in (1, 3, 6):
+        out = _host_eval(PRIVATE_BODY, x, PRIVATE_HELPERS, calls=calls)
+        for row, t in zip(out, x[:, 12]):
+            vals = [np.float32(t) * np.float32(c) for c in range(1, calls + 1)]
+            acc_x = np.float32(0)
+            for v in vals:
+                acc_x = np.float32(acc_x + v)
+            hist = [0.0] * 4
+            for c, v in enumerate(vals, start=1):
+                hist[c % 4] = v
+            h = np.float32(np.float32(np.float32(hist[0] + hist[1]) + hist[2]) + hist[3])
+            np.testing.assert_array_equal(row, [acc_x + h, np.float32(calls) + np.float32(calls), 0.0])
+    assert "linon_multi_fk" in validate_field(PRIVATE_BODY, PRIVATE_HELPERS, batched=True)
+
+
+@pytest.mark.parametrize("helpers,needle", [
+    ("var<workgroup> w: f32;", "only var<private>"),
+    ("var<private> w;", "needs a type or an initializer"),
+    ("var<private> w: f32 = 1.0;\nconst c = w * 2.0;\nfn f() -> f32 { return c; }", "module initializers must be constant"),
+    ("var<private> w: f32 = 1.0;\nvar<private> z: f32 = w;", "module initializers must be constant"),
+])
+def test_private_variable_diagnostics(helpers, needle):
+    with pytest.raises(_abi.LinonCompileError) as e:
+        translate_wgsl("return p;", helpers)
+    assert needle in e.value.message, e.value.message

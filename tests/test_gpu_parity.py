@@ -612,6 +612,49 @@ def test_row_shards_equal_whole_frame(engine):
     engine.render_rows(fld, w.camera, st, params, full, 7, 7)  # empty range: nothing to do
 
 
+def test_private_state_is_per_ray(engine):
+    """var<private> lives for one ray: a field that counts its calls and
+    turns back after 40 of them (10 RK4 steps) brings every ray of a
+    20-step march back to the eye, in the per-frame kernel and in a batch
+    (which then uses the one-CTA-per-tile schedule), next to a stateless
+    field in the same batch."""
+    helpers = "var<private> calls: u32 = 0u;"
+    body = "calls += 1u;\nif (calls > 40u) { return -v0; }\nreturn v0;"
+    w = wl.plain_small(40, 30)
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    params = wl.fixed_steps(0.05, 20, kahan=True)
+    fld = engine.compile_field(body, helpers)
+    planes = FramePlanes.allocate(w.width, w.height)
+    engine.render(fld, w.camera, w.settings, params, planes)
+    engine.synchronize()
+    eye = np.array(list(w.camera.origin)[:3], np.float32)
+    ends = planes.mapping.cpu().numpy()[..., :3]
+    assert np.abs(ends - eye).max() < 1e-4
+    # batched next to a stateless field: per-view plain launches = batch
+    flds = [fld, field(engine, "linear", False)]
+    views, outs = [], []
+    for k in range(4):
+        fp = FramePlanes.allocate(24 + 8 * k, 16 + 4 * k)
+        v = _abi.View()
+        v.camera, v.settings, v.params = w.camera, w.settings, params
+        v.width, v.height, v.field_index = fp.width, fp.height, k % 2
+        v.out = fp.abi()
+        views.append(v)
+        outs.append(fp)
+    engine.render_views_plain(flds, views)
+    a = snapshot(outs)
+    for tuning in (None, _abi.BatchTuning(1024, 128, 0, 4, 8, 0, 1)):  # a persistent request is overridden
+        for fp in outs:
+            fp.mapping.zero_()
+        engine.render_batch(flds, views, tuning)
+        engine.synchronize()
+        b = snapshot(outs)
+        for k, (x, y) in enumerate(zip(a, b)):
+            np.testing.assert_allclose(y["mapping"], x["mapping"], rtol=0, atol=1e-5)
+            if k % 2 == 0:
+                assert np.abs(y["mapping"][..., :3] - eye).max() < 1e-4
+
+
 def test_hbm_budget_admission():
     from linon_gb300 import Engine
     e = Engine(0, hbm_budget=1 << 20)
