@@ -1226,7 +1226,7 @@ def test_fuzzed_fields_never_crash_and_compile_when_accepted():
     pool = [(predefined_source(i), None) for i in range(1, 15)]
     pool += [(POINTER_BODY, POINTER_HELPERS), (NESTED_BODY, NESTED_HELPERS),
              (ALIAS_OVERRIDE_BODY, ALIAS_OVERRIDE_HELPERS), (ALL_NEW_BUILTINS_BODY, None),
-             (SWITCH_BODY, None), (STRUCT_BODY, STRUCT_HELPERS)]
+             (SWITCH_BODY, None), (STRUCT_BODY, STRUCT_HELPERS), (PRIVATE_BODY, PRIVATE_HELPERS)]
     toks = ["(", ")", ";", ",", ".", "&", "*", "-", "!", "~", "+", "%", "/", "<<", ">>", "^", "|", "&&", "==", "<",
             "let", "var", "1", "1.5", "2u", "-3", "p", "v", "t", "x", "i32", "f32", "u32", "vec2", "vec3<i32>",
             "vec3<u32>", "select", "abs", "max", "dot", "countOneBits", "frexp", "[0]", ".xy", "true"]
