@@ -1163,7 +1163,8 @@ def test_every_accepted_operator_combination_compiles():
     assert len(lines) == 136
     body = "\n".join(lines) + "\nreturn p;"
     _host_eval(body, np.zeros((2, 13), np.float32))           # compiles for the host
-    assert "linon_march_v14" in validate_field(body)          # and for the GPU
+    assert "linon_march_v14" in validate_field(body)          # and for the GPU, fast
+    assert "linon_march_v1" in validate_field(body, precise=True)  # and precise modules
 
 
 def test_every_accepted_builtin_call_compiles():
@@ -1193,6 +1194,7 @@ def test_every_accepted_builtin_call_compiles():
     body = "\n".join(lines) + "\nreturn p;"
     _host_eval(body, np.zeros((2, 13), np.float32))
     assert "linon_march_v14" in validate_field(body)
+    assert "linon_march_v1" in validate_field(body, precise=True)
     v = _host_eval("return vec3<f32>(f32(dot(vec4<i32>(1, -2, 3, 4), vec4<i32>(5, 6, -7, 8))),"
                    " f32(dot(vec2<u32>(3u, 4u), vec2<u32>(5u, 6u))), 0.0);", np.zeros((1, 13), np.float32))
     np.testing.assert_array_equal(v[0], [5 - 12 - 21 + 32, 39, 0])
