@@ -665,7 +665,8 @@ int render_checks(linon_ctx* ctx, const linon_field* field, const linon_camera* 
 }
 
 // One launch of the plain march kernel over rows [row0, row1) of the frame
-// (row0 a multiple of the 16-row tile).
+// (any rows: the 8x16 tiles start at row0, and a pixel's ray depends on its
+// own row and column alone).
 int launch_rows(linon_ctx* ctx, const linon_field* field, const linon_camera* camera,
                 const linon_settings* settings, const linon_march_params* params, const linon_frame* out,
                 int row0, int row1, cudaStream_t stream) {
