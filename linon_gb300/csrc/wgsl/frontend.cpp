@@ -2032,7 +2032,7 @@ class Compiler {
       if (r->kind == Expr::Name && !roots.insert(r->op).second)
         fail(a->line, a->col, "two pointer arguments of '" + f.name + "' refer to '" + r->op + "' (aliasing)");
     }
-    ci.fn = "u_" + f.name;
+    ci.fn = f.name == "field_function" ? f.name : "u_" + f.name;
     e.ty = f.has_ret ? f.ret : voidT();
     e.fl += f.fl;
     e.tr += f.tr;
@@ -2585,7 +2585,7 @@ class Compiler {
           }
           default:
             // user functions also receive the invocation's private variables
-            if (ci.fn.compare(0, 2, "u_") == 0) return ci.fn + "(pv" + (as.empty() ? "" : ", ") + join(0) + ")";
+            if (ci.fn.compare(0, 2, "u_") == 0 || ci.fn == "field_function") return ci.fn + "(pv" + (as.empty() ? "" : ", ") + join(0) + ")";
             return ci.fn + "(" + join(0) + ")";
         }
       }
@@ -3066,9 +3066,9 @@ Translation translate(const std::string& field_body, const std::string& helpers_
     os << "struct Private {\n";
     for (auto& m : cc.private_code) os << m << "\n";
     os << "};\n";
-    // prototypes (WGSL functions may be used before their declaration)
+    // prototypes (WGSL functions may be used before their declaration; a
+    // helper may call the field function, as the shader's march loop does)
     for (auto& f : cc.fns) {
-      if (f->name == "field_function") continue;
       std::string sig = f->code.substr(0, f->code.find('{'));
       os << sig << ";\n";
     }

@@ -19,11 +19,13 @@
 // -ffp-contract=off and without -ffast-math), `double` the FP64 accuracy
 // oracle, `CountingFloat` counts FP32 operations per ray step.
 //
-// Parity status: UNPINNED against the reference itself.  The reference is
-// WGSL executed through wgpu/naga on a graphics API; neither a graphics stack
-// nor a Rust toolchain exists where this project is built or measured, and the
-// reference ships no tests, golden vectors or fixtures for this path.  The
-// pins that do exist are listed in tests/golden/README.md.
+// Parity status: pinned against the reference's shader source, not its
+// runtime.  The reference is WGSL executed through wgpu/naga on a graphics
+// API; neither a graphics stack nor a Rust toolchain exists where this project
+// is built or measured, and the reference ships no tests, golden vectors or
+// fixtures for this path.  Its shader text itself, lowered on the host with
+// the bindings made private, gives the fixtures this file is held to bit for
+// bit; they and the other pins are listed in tests/golden/README.md.
 //
 // Where WGSL leaves the result implementation-defined, this file fixes one
 // choice and the CUDA engine follows it:

@@ -1319,3 +1319,43 @@ def test_private_variable_diagnostics(helpers, needle):
     with pytest.raises(_abi.LinonCompileError) as e:
         translate_wgsl("return p;", helpers)
     assert needle in e.value.message, e.value.message
+
+
+CALLER_HELPERS = """
+var<private> n: u32;
+fn euler(p0: vec3<f32>, v0: vec3<f32>, h: f32) -> vec3<f32> {
+  var p = p0;
+  for (var i = 0; i < 3; i++) {
+    p = p + h * field_function(p, p, v0, v0, f32(i));
+  }
+  return p;
+}
+"""
+
+
+def test_helper_calls_the_field_function():
+    """A helper may call the field function (the shader's own march loop,
+    main_view.wgsl:229-279, is such a helper); the call passes the
+    invocation's private state, and a cycle through the field function is
+    rejected as recursion."""
+    code = translate_wgsl("n += 1u;\nreturn v * 2.0 + vec3<f32>(t, f32(n), 0.0);", CALLER_HELPERS)
+    src = "\n".join([f'#include "{RT}"', code,
+                     'extern "C" void run(float* out) {',
+                     "  linon_user::Private pv;",
+                     "  wgsl::vec3f r = linon_user::u_euler(pv, wgsl::vec3f(1.f, 2.f, 3.f), wgsl::vec3f(0.5f, 0.f, 1.f), 0.25f);",
+                     "  out[0] = r.x; out[1] = r.y; out[2] = r.z; out[3] = float(pv.u_n); }"])
+    d = Path(tempfile.mkdtemp(prefix="linon_fe2_"))
+    (d / "f.cpp").write_text(src)
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-shared", "-fPIC", "-o", str(d / "f.so"),
+                        str(d / "f.cpp")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    out = np.zeros(4, np.float32)
+    C.CDLL(str(d / "f.so")).run(C.c_void_p(out.ctypes.data))
+    p = np.float32([1, 2, 3])
+    for i in range(3):
+        k = np.float32([0.5, 0, 1]) * np.float32(2) + np.float32([i, i + 1, 0])
+        p = (p + np.float32(0.25) * k).astype(np.float32)
+    np.testing.assert_array_equal(out, list(p) + [3.0])
+    with pytest.raises(_abi.LinonCompileError) as e:
+        translate_wgsl("return euler(p, v, 0.1);", CALLER_HELPERS)
+    assert "recursion" in str(e.value)
