@@ -74,6 +74,32 @@ def predefined_bodies(ref: Path) -> dict:
     return out
 
 
+def rust_array(src: str, name: str, dtype) -> np.ndarray:
+    """The literal `pub const NAME: [T; N] = [...];` of a Rust file."""
+    m = re.search(rf"pub const {name}: \[\w+; (\d+)\] = \[(.*?)\];", src, re.S)
+    if not m:
+        raise SystemExit(f"no array {name}")
+    items = [t for t in re.sub(r"//[^\n]*", "", m.group(2)).replace("\n", " ").split(",") if t.strip()]
+    a = np.array([float(t) for t in items], dtype)
+    if len(a) != int(m.group(1)):
+        raise SystemExit(f"{name}: {len(a)} items, declared {m.group(1)}")
+    return a
+
+
+def scene_digest(ref: Path) -> str:
+    """src/cornell_box.rs's VERTICES and INDICES must equal this package's
+    raw Cornell box (scene.cornell_raw); returns the SHA-256 of their bytes,
+    which the tests check against the package without the reference."""
+    import hashlib
+    src = (ref / "src" / "cornell_box.rs").read_text()
+    v = rust_array(src, "VERTICES", np.float32).reshape(-1, 3)
+    f = rust_array(src, "INDICES", np.float64).astype(np.uint32).reshape(-1, 3)
+    xyz, faces, _ = scene.cornell_raw()
+    if not (np.array_equal(v, xyz) and np.array_equal(f, faces)):
+        raise SystemExit("scene.cornell_raw differs from src/cornell_box.rs")
+    return hashlib.sha256(v.tobytes() + f.tobytes()).hexdigest()
+
+
 def f32s(a) -> str:
     return ", ".join(repr(float(np.float32(x))) for x in np.asarray(a, np.float32).ravel())
 
@@ -286,6 +312,7 @@ def main():
     settings_f = np.array([1.0, 0.3, 0.6, 0.0], np.float32)  # field_weight, mouse x, mouse y, lyapunov_scaling
     settings_i = np.array([0, 1], np.int32)                 # overlay_mode, central_difference_delta
     data = {"scene/xyz": xyz, "scene/faces": faces, "scene/camera": camera,
+            "scene/raw_sha256": np.array(scene_digest(ref)),
             "main/settings_f": settings_f, "main/settings_i": settings_i}
     sample_gids = np.array([[x, 0] for x in range(8)], np.int32)
 

@@ -55,6 +55,15 @@ def main_setup(g):
     return xyz, faces, camera, st
 
 
+def test_scene_is_the_reference_box(pins):
+    """scene.cornell_raw equals src/cornell_box.rs's VERTICES and INDICES
+    (compared by the fixture script; here through the digest it stored)."""
+    import hashlib
+    xyz, faces, _ = scene.cornell_raw()
+    digest = hashlib.sha256(xyz.astype(np.float32).tobytes() + faces.astype(np.uint32).tobytes()).hexdigest()
+    assert digest == str(pins["scene/raw_sha256"])
+
+
 def pixel_index(gids, W, H):
     return ((H - 1 - gids[:, 1]) * W + gids[:, 0]).astype(np.int32)
 
