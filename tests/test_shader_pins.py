@@ -141,3 +141,28 @@ def test_overlay(oracle, pins, case):
     want_e = pins[f"overlay/{case}/exponents"]
     np.testing.assert_array_equal(e.view(np.uint32), want_e.view(np.uint32))  # -1 where nothing was written
     np.testing.assert_array_equal(out, unorm8(pins[f"overlay/{case}/color"]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("field", ["identity", "lorenz", "roessler", "translation_x", "mirage_plane"])
+def test_engine_equals_shader_source(engine, pins, field):
+    """The CUDA engine (precise module, through the C ABI) against the
+    shader-source fixtures directly: endpoints bit for bit, colour within
+    1/255 (the specular pow is CUDA's)."""
+    import torch
+    from linon_gb300 import FramePlanes
+    from linon_gb300.engine import predefined_source
+    xyz, faces, camera, st = main_setup(pins)
+    engine.upload_scene(xyz, faces, None, bvh=True)
+    fld = engine.compile_field(predefined_source(_abi.FIELD_IDS[field]), precise=True)
+    W, H = 48, 40
+    planes = FramePlanes.allocate(W, H)
+    engine.render(fld, camera, st, _abi.reference_params(), planes)
+    engine.synchronize()
+    torch.cuda.synchronize()
+    pix = pixel_index(pins[f"view/{field}/gids"], W, H)
+    mapping = planes.mapping.cpu().numpy().reshape(-1, 4)[pix]
+    color = planes.color.cpu().numpy().reshape(-1, 4)[pix]
+    np.testing.assert_array_equal(mapping.view(np.uint32), pins[f"view/{field}/mapping"].view(np.uint32))
+    want = unorm8(pins[f"view/{field}/color"]).astype(np.int32)
+    assert np.abs(color.astype(np.int32) - want).max() <= 1
