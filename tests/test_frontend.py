@@ -1356,6 +1356,9 @@ def test_helper_calls_the_field_function():
         k = np.float32([0.5, 0, 1]) * np.float32(2) + np.float32([i, i + 1, 0])
         p = (p + np.float32(0.25) * k).astype(np.float32)
     np.testing.assert_array_equal(out, list(p) + [3.0])
+    body = "n += 1u;\nreturn v * 2.0 + vec3<f32>(t, f32(n), 0.0);"
+    assert "linon_march_v14" in validate_field(body, CALLER_HELPERS)  # NVRTC, sm_103a
+    assert "linon_multi_fk" in validate_field(body, CALLER_HELPERS, batched=True)
     with pytest.raises(_abi.LinonCompileError) as e:
         translate_wgsl("return euler(p, v, 0.1);", CALLER_HELPERS)
     assert "recursion" in str(e.value)
