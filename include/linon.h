@@ -305,18 +305,19 @@ int linon_capture_paths(linon_ctx* ctx, const linon_field* field,
 /* Path capture that allocates nothing.  No counterpart in the reference.
  * For callers that cannot allocate device memory: a click handler on an
  * interactive UI thread with a frame budget (an allocation or free can
- * synchronise the whole device), code recording its work into a CUDA graph
- * (allocation calls cannot be captured), or a host that gave the context a
- * fixed memory budget.  Same arguments and output as linon_capture_paths;
+ * synchronise the whole device), or a host that gave the context a fixed
+ * memory budget.  Same arguments, checks and output as linon_capture_paths;
  * the start positions are staged in a fixed device array inside the library
  * (LINON_NOALLOC_MAX_RAYS rays, 128 KB, held on every GPU that loads the
  * library until the process exits) instead of the context's scratch buffer,
  * and no cudaMalloc/cudaFree or other allocating routine is called.
- * n_rays > LINON_NOALLOC_MAX_RAYS fails with LINON_EINVAL.  The first call on
- * a device looks up the array's device address (set-up done once per
- * device); make that first call before any stream capture.  Every call shares
- * the one array: calls whose work overlaps on the GPU (other streams or
- * contexts) race on it and must be serialised by the caller.               */
+ * n_rays > LINON_NOALLOC_MAX_RAYS fails with LINON_EINVAL.  pos_xy is
+ * ordinary (pageable) host memory, read before the call returns.  The first
+ * call on a device looks up the array's device address (set-up done once per
+ * device); make that first call before any stream capture, and do not use
+ * the library across a cudaDeviceReset.  Every call shares the one array:
+ * calls whose work overlaps on the GPU (other streams or contexts) race on
+ * it and must be serialised by the caller.                                  */
 #define LINON_NOALLOC_MAX_RAYS 16384
 int linon_capture_paths_noalloc(linon_ctx* ctx, const linon_field* field,
                                 const linon_camera* camera,

@@ -219,3 +219,19 @@ def reference_params() -> MarchParams:
     p = MarchParams()
     load().linon_march_params_reference(C.byref(p))
     return p
+
+
+def shader_params() -> MarchParams:
+    """The shader's own march constants, filled in Python without loading
+    liblinon.so: h = 0.1 (main_view.wgsl:241), the t <= 5 loop (:244),
+    adaptive refinement to h = 0.001 above h = 0.002 (:252-253), focal
+    length 0.035 and viewport height 0.025 (:355-356).  Equal field for
+    field to linon_march_params_reference (a CPU test holds them equal);
+    the workload builders use it so that the CPU reference leg never maps
+    the engine library."""
+    p = MarchParams()
+    p.h_initial, p.t_max, p.max_steps, p.adaptive = 0.1, 5.0, 0, 1
+    p.h_fine, p.h_fine_above = 0.001, 0.002
+    p.stop_on_hit, p.kahan, p.linear_mode, p.reserved = 0, 0, 0, 0
+    p.focal_length, p.viewport_height = 0.035, 0.025
+    return p

@@ -336,6 +336,10 @@ DevScene dev_scene(const linon_ctx* ctx) {
   s.reach = ctx->reach;
   return s;
 }
+
+int check_context(linon_ctx* ctx) { return enter(ctx); }
+int check_field(const linon_ctx* ctx, const linon_field* f) { return field_valid(ctx, f); }
+int check_image_size(int32_t W, int32_t H) { return check_frame_size(W, H); }
 }  // namespace linon
 
 extern "C" {

@@ -83,6 +83,13 @@ void build_scene_arrays(const float* xyz, uint32_t nv, const uint32_t* abc, uint
 // Scene pointers and parameters of a context for the kernels (api.cpp).
 DevScene dev_scene(const linon_ctx* ctx);
 
+// Argument checks shared by the entry points (api.cpp): a non-null context
+// whose device is made current; a live field of that context; an image of
+// 1..65535 pixels per side and at most 2^31-1 pixels.
+int check_context(linon_ctx* ctx);
+int check_field(const linon_ctx* ctx, const linon_field* f);
+int check_image_size(int32_t W, int32_t H);
+
 // Frees the batch tables, graphs and modules of a context (batch.cpp).
 void batch_release(linon_ctx* ctx);
 

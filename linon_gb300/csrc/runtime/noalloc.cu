@@ -4,10 +4,9 @@
 // scratch buffer, which it grows with cudaMalloc when a call needs more.  Some
 // callers must not trigger that: a click handler on an interactive UI thread
 // with a frame budget (a device allocation or free can synchronise the whole
-// device), code that records its work into a CUDA graph (allocation calls
-// cannot be captured), or a host that has given the context a fixed memory
-// budget.  This entry point stages the positions in a fixed array inside the
-// library instead, so it allocates nothing.
+// device), or a host that has given the context a fixed memory budget.  This
+// entry point stages the positions in a fixed array inside the library
+// instead, so it allocates nothing.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -36,7 +35,10 @@ std::mutex g_mu;
 float* g_positions_dev[kMaxDevices] = {nullptr};
 
 // Device address of the array on the current device, looked up once per
-// device (the first call on a device does this set-up).
+// device (the first call on a device does this set-up).  The address belongs
+// to the device's primary context: a cudaDeviceReset ends that context, and
+// with it every linon context on the device and this set-up, so the library
+// must not be used across a device reset.
 int positions_address(int device, float** out) {
   if (device < 0 || device >= kMaxDevices) return set_error(LINON_EINVAL, "device index out of range");
   std::lock_guard<std::mutex> lock(g_mu);
@@ -61,14 +63,11 @@ extern "C" int linon_capture_paths_noalloc(linon_ctx* ctx, const linon_field* fi
                                            int32_t height, const float* pos_xy, int32_t n_rays, float h,
                                            int32_t n_steps, int32_t record_every, float* out) {
   try {
-    if (!ctx) return set_error(LINON_EINVAL, "null context");
-    cudaError_t e = cudaSetDevice(ctx->device);
-    if (e != cudaSuccess) return cuda_error(e, "cudaSetDevice");
-    if (!field || !field->mod) return set_error(LINON_EINVAL, "null or released field");
-    if (field->ctx != ctx) return set_error(LINON_EINVAL, "field belongs to another context");
+    // the same checks as linon_capture_paths, then the array's limit
+    if (int st = check_context(ctx)) return st;
+    if (int st = check_field(ctx, field)) return st;
     if (!camera || !params || !pos_xy || !out) return set_error(LINON_EINVAL, "null capture argument");
-    if (width <= 0 || height <= 0 || width > 65535 || height > 65535)
-      return set_error(LINON_EINVAL, "image size must be in 1..65535 per side");
+    if (int st = check_image_size(width, height)) return st;
     if (n_rays <= 0) return set_error(LINON_EINVAL, "n_rays must be positive");
     if (n_rays > kNoAllocMaxRays)
       return set_error(LINON_EINVAL, "n_rays " + std::to_string(n_rays) + " exceeds the " +
@@ -79,8 +78,9 @@ extern "C" int linon_capture_paths_noalloc(linon_ctx* ctx, const linon_field* fi
     if (!(h > 0.0f) || !std::isfinite(h)) return set_error(LINON_EINVAL, "h must be positive");
     float* pos_dev = nullptr;
     if (int st = positions_address(ctx->device, &pos_dev)) return st;
-    e = cudaMemcpyAsync(pos_dev, pos_xy, sizeof(float) * 2 * size_t(n_rays), cudaMemcpyHostToDevice,
-                        ctx->stream);
+    // pos_xy is pageable host memory: the copy has read it when this returns
+    cudaError_t e = cudaMemcpyAsync(pos_dev, pos_xy, sizeof(float) * 2 * size_t(n_rays),
+                                    cudaMemcpyHostToDevice, ctx->stream);
     if (e != cudaSuccess) return cuda_error(e, "cudaMemcpyAsync (positions)");
     CaptureArgs a;
     std::memset(&a, 0, sizeof a);

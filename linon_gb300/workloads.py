@@ -39,7 +39,7 @@ def settings(field_weight=1.0, mouse=(0.5, 0.6), overlay_mode=0, delta=1, scalin
 
 def fixed_steps(h: float, steps: int, kahan: bool = False, stop_on_hit: bool = False,
                 vfov: float = 45.0) -> _abi.MarchParams:
-    p = _abi.reference_params()
+    p = _abi.shader_params()
     p.h_initial = h
     p.max_steps = steps
     p.adaptive = 0
@@ -67,7 +67,7 @@ class Workload:
 def reference_default(width=512, height=512, field=_abi.FIELD_IDS["mirage_spherical_sigmoid"]) -> Workload:
     xyz, faces, _, center = scene.cornell_reference()
     return Workload("reference_default", xyz, faces, None, width, height, cam.arcball_default(center),
-                    settings(), _abi.reference_params(), [field])
+                    settings(), _abi.shader_params(), [field])
 
 
 def plain_small(width=512, height=512) -> Workload:
@@ -146,5 +146,5 @@ def obj_scene(width=256, height=192, model: int = 0, text: str | None = None) ->
     model=1 is the torus with the two panels)."""
     m = scene.parse_obj(text or obj_scene_text(), model=model, normalize=True)
     return Workload(f"obj_scene_model{model}_{width}x{height}", m.xyz, m.faces, None, width, height,
-                    cam.arcball_default(m.center), settings(), _abi.reference_params(),
+                    cam.arcball_default(m.center), settings(), _abi.shader_params(),
                     [_abi.FIELD_IDS["mirage_spherical_sigmoid"]], extra={"n_models": m.n_models})

@@ -24,8 +24,9 @@
 // API; neither a graphics stack nor a Rust toolchain exists where this project
 // is built or measured, and the reference ships no tests, golden vectors or
 // fixtures for this path.  Its shader text itself, lowered on the host with
-// the bindings made private, gives the fixtures this file is held to bit for
-// bit; they and the other pins are listed in tests/golden/README.md.
+// the bindings made private (tests/golden/make_shader_pins.py), gives the
+// fixtures this file is held to bit for bit (tests/golden/shader_pins.npz,
+// checked by tests/test_shader_pins.py).
 //
 // Where WGSL leaves the result implementation-defined, this file fixes one
 // choice and the CUDA engine follows it:

@@ -3,9 +3,10 @@
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
 CPU-baseline leg of bench.py as the oracle the CUDA engine is compared
 against; never as the thing measured or shipped.  The oracle is the C++ restatement of the shader
-path in oracle/linon_oracle.hpp (pinned bit for bit against the reference's
-shader source lowered on the host, tests/golden/README.md; the reference's
-runtime, WGSL through a graphics API, is not available here).
+path in oracle/linon_oracle.hpp, pinned bit for bit against the reference's
+shader source lowered on the host (tests/golden/make_shader_pins.py writes the
+fixtures, tests/test_shader_pins.py checks them); the reference's runtime,
+WGSL through a graphics API, is not available where this runs.
 """
 from __future__ import annotations
 

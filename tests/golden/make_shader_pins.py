@@ -15,7 +15,7 @@ private state.  Every substitution is a literal string replacement that
 must match; a changed reference fails loudly.
 
 Run from the repository root, where the reference sources are present:
-    python tests/golden/make_shader_pins.py [reference_root]
+    python tests/golden/make_shader_pins.py <path of the linon source tree>
 """
 from __future__ import annotations
 
@@ -303,7 +303,9 @@ def outline_exponents(W, H):
 
 
 def main():
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python tests/golden/make_shader_pins.py <path of the linon source tree>")
+    ref = Path(sys.argv[1])
     bodies = predefined_bodies(ref)
     xyz, faces, camera = scene_arrays()
     if len(xyz) > MAX_VERTICES or len(faces) > MAX_FACES:

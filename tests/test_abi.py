@@ -60,6 +60,23 @@ def test_reference_params(lib):
     assert (p.h_initial, p.t_max, p.max_steps, p.adaptive) == (pytest.approx(0.1), 5.0, 0, 1)
     assert (p.h_fine, p.h_fine_above) == (pytest.approx(0.001), pytest.approx(0.002))
     assert (p.focal_length, p.viewport_height) == (pytest.approx(0.035), pytest.approx(0.025))
+    # the Python restatement the workload builders (and the CPU reference
+    # leg of bench.py) use is byte-identical to the library's defaults
+    assert bytes(_abi.shader_params()) == bytes(p)
+
+
+def test_reference_leg_does_not_map_the_engine_library():
+    # building the benchmark workloads and the oracle's inputs must not load
+    # liblinon.so (the CPU reference leg stands alone)
+    import subprocess
+    import sys
+    code = ("import sys; sys.path.insert(0, '.');"
+            "from linon_gb300 import workloads as wl, _abi;"
+            "w = wl.frames_1080p(); v = wl.batch_uneven(64); l = wl.lyapunov_1024(); s = wl.plain_small();"
+            "maps = open('/proc/self/maps').read();"
+            "assert _abi._lib is None and 'liblinon.so' not in maps, 'engine library mapped'")
+    r = subprocess.run([sys.executable, "-c", code], cwd=str(_abi._PKG.parent), capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
 
 
 def test_status_strings_and_predefined(lib):

@@ -1,13 +1,14 @@
 """linon_capture_paths_noalloc: ray-path capture that allocates nothing.
 
 Callers that cannot allocate device memory (an interactive click handler with
-a frame budget, work recorded into a CUDA graph, a host with a fixed memory
-budget) use this variant; it stages the ray start positions in a fixed array
-inside the library instead of the context's scratch buffer.  Checked here
-through the C ABI against linon_capture_paths on two calls in a row (the
-second with fewer rays, so stale positions from the first call are present in
-the shared array), plus the size limit.  This file sorts last so that a run
-stopping at the first failure has already run every other test.
+a frame budget, a host with a fixed memory budget) use this variant; it stages
+the ray start positions in a fixed array inside the library instead of the
+context's scratch buffer.  Checked here through the C ABI against
+linon_capture_paths on two calls in a row (the second with fewer rays, so
+stale positions from the first call are present in the shared array), plus
+the size limit and the image-size checks both entry points share.  This file
+sorts last so that a run stopping at the first failure has already run every
+other test.
 """
 import ctypes as C
 
@@ -59,3 +60,20 @@ def test_noalloc_rejects_more_rays_than_the_array_holds(engine):
     st = _call(lib, engine, fld, w, pos, 0.01, 10, 1, out)
     assert st == _abi.LINON_EINVAL
     assert b"16384" in lib.linon_last_error()
+
+
+def test_noalloc_checks_image_size_like_capture_paths(engine):
+    # 65535 x 65535 is within the per-side limit but above 2^31-1 pixels:
+    # both entry points reject it before any work is queued
+    lib = _abi.load()
+    w = wl.plain_small(64, 64)
+    fld = engine.compile_field(predefined_source(_abi.FIELD_IDS["linear"]))
+    w.width = w.height = 65535
+    pos = np.full((4, 2), 0.5, np.float32)
+    out = torch.zeros((1, 4), dtype=torch.float32, device="cuda")  # never written
+    assert _call(lib, engine, fld, w, pos, 0.01, 10, 1, out) == _abi.LINON_EINVAL
+    msg = lib.linon_last_error()
+    st = lib.linon_capture_paths(engine.ctx, fld.handle, C.byref(w.camera), C.byref(w.settings), C.byref(w.params),
+                                 w.width, w.height, pos.ctypes.data, len(pos), 0.01, 10, 1, out.data_ptr())
+    assert st == _abi.LINON_EINVAL
+    assert lib.linon_last_error() == msg
