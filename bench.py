@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
@@ -110,19 +111,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def flops_per_step(wl_mod, pyoracle, w, fid):
-    """Algorithmic FP32 operations of one accepted RK4 step (field evaluations,
-    RK4 bookkeeping, blend, Kahan sums), counted by the oracle's counting
-    float on an empty scene (intersection work excluded: the BVH culls it and
-    brute-force-equivalent FLOPs are not claimed)."""
-    import numpy as _np
-    pix = _np.array([w.width // 2 + (w.height // 2) * w.width, 17 + 11 * w.width], _np.int32)
-    p = wl_mod.fixed_steps(w.params.h_initial, 64, kahan=bool(w.params.kahan))
-    ops, steps = pyoracle.count_ops(_np.zeros((0, 3), _np.float32), _np.zeros((0, 3), _np.uint32), w.camera,
-                                    w.settings, p, fid, w.width, w.height, pix)
-    arith = (ops[:, 0] + ops[:, 1] + ops[:, 2] + ops[:, 3]).astype(float) / steps
-    transc = ops[:, 5].astype(float) / steps
-    return float(arith.mean()), float(transc.mean())
+def flops_per_step(pyoracle, w, fid):
+    """Algorithmic FP32 operations of one accepted RK4 step: the operations
+    the ray's endpoint depends on (oracle TraceFloat liveness), without
+    loop-invariant work or products by launch constants, on an empty scene
+    (intersection work excluded: the BVH culls it and brute-force-equivalent
+    FLOPs are not claimed).  Returns (arithmetic ops, transcendental calls)
+    per step; every + - * / sqrt counts 1, so an FMA is 2."""
+    pix = np.array([w.width // 2 + (w.height // 2) * w.width, 17 + 11 * w.width], np.int32)
+    live = pyoracle.count_live_ops(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32), w.camera,
+                                   w.settings, w.params, fid, w.width, w.height, pix)
+    return float(live[:, :4].sum(axis=1).mean()), float(live[:, 4].mean())
 
 
 def cpu_baseline(pyoracle, w, budget_s=12.0):
@@ -173,10 +172,11 @@ def cpu_views_sample(pyoracle, views, w, budget_s=4.0):
     return steps / dt, threads, f"{rays} rays ({threads} per view) of {done} views, brute-force faces, {dt:.1f} s"
 
 
-def bench_configs(eng, wl, predefined_source, pyoracle, cpu):
+def bench_configs(eng, wl, predefined_source, pyoracle, cpu, keep=None):
     """The other workloads' GPU and CPU numbers: the 512^2 twist frame (h
     0.01 x 1000 steps), and the oracle on bounded samples of it, of the
-    1024^2 Lyapunov render and of the 64 uneven views."""
+    1024^2 Lyapunov render and of the 64 uneven views.  keep: receives the
+    512^2 frame's planes for the accuracy leg."""
     import torch
     out = {}
     w = wl.plain_small()
@@ -197,6 +197,8 @@ def bench_configs(eng, wl, predefined_source, pyoracle, cpu):
     steps = int(planes.steps.sum().item())
     ms = statistics.median(ts)
     out["plain_512_twist"] = {"workload": w.name, "frame_ms": ms, "ray_steps_per_s": steps / (ms * 1e-3)}
+    if keep is not None:
+        keep["plain_512_twist"] = (w, planes)
     if cpu:
         v, th, smp = cpu_baseline(pyoracle, w, budget_s=3.0)
         out["plain_512_twist"]["cpu"] = {"value": v, "unit": UNIT, "cores": th, "kind": "port", "sample": smp}
@@ -356,35 +358,42 @@ def main():
     # ---- roofline: FP32 against a measured FFMA peak ----
     if rank == 0:
         peak = eng.probe_fp32_peak()
-        fl = [flops_per_step(wl, pyoracle, w, fid) for fid in w.fields]
+        fl = [flops_per_step(pyoracle, w, fid) for fid in w.fields]
+        n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
         # dominant kernel: the march launch with the largest median time
         i = int(np.argmax(per_field_ms))
         achieved = fl[i][0] * steps_per_frame[i] / (per_field_ms[i] * 1e-3) / 1e12
-        traffic = None
-        tfile = ROOT / "profiles" / "march_traffic.json"
-        if tfile.exists():
-            try:
-                traffic = json.loads(tfile.read_text()).get(["linear", "twist", "lens"][i])
-            except Exception:
-                traffic = None
         result["roofline"] = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                              "frac": achieved / peak, "traffic": traffic,
+                              "frac": achieved / peak, "traffic": None,
+                              "traffic_note": "DRAM bytes per launch are in profiles/ (ncu); the 58 MB of "
+                                              "output planes are still L2-resident when the launch ends",
                               "kernel": f"linon_march_v14 ({['linear', 'twist', 'lens'][i]} field; "
                                         "fixed steps, Kahan, field_weight 1)",
                               "peak_source": "measured FFMA probe in this run (linon_probe_fp32_peak)",
+                              "peak_nominal_at_median_clock": (n_sm * 128 * 2 * clk["sm_mhz"] * 1e6 / 1e12
+                                                               if clk.get("sm_mhz") else None),
+                              "peak_nominal_formula": f"{n_sm} SMs x 128 FP32 lanes x 2 (FMA) x median SM clock",
+                              "flops_definition": "live FP32 operations per ray-step (oracle TraceFloat)",
                               "flops_per_step": {n: round(a, 2) for n, (a, _) in zip(["linear", "twist", "lens"], fl)},
                               "transcendentals_per_step": {n: round(t, 2) for n, (_, t) in
                                                            zip(["linear", "twist", "lens"], fl)},
                               "all_fields_frac": sum(a * s for (a, _), s in zip(fl, steps_per_frame))
                               / (sum(per_field_ms) * 1e-3) / 1e12 / peak}
 
+    # engine planes of the headline frames at the accuracy leg's pixels
+    keep = {}
+    if rank == 0 and not args.no_accuracy:
+        from oracle import accuracy as acc
+        pix = acc.sample_pixels(w.width, w.height, 4000, seed=11)
+        keep["frames_1080p"] = (w, pix, [p.sample(pix) for p in planes])
+
     # ---- batched persistent kernel vs plain per-view kernel (64 views) ----
     if rank == 0 and not args.no_batch:
-        result["batch_uneven_64"] = bench_batch(eng, stream, wl, torch, dev, predefined_source)
+        result["batch_uneven_64"] = bench_batch(eng, stream, wl, torch, dev, predefined_source, keep)
 
     # ---- Lyapunov pipeline at 1024^2 (scaled Lorenz + v0, h 0.002 x 2000) ----
     if rank == 0 and not args.no_batch:
-        result["lyapunov_1024"] = bench_lyapunov(eng, wl, predefined_source)
+        result["lyapunov_1024"] = bench_lyapunov(eng, wl, predefined_source, keep)
 
     # ---- serving: Poisson request stream, continuous batching ----
     if rank == 0 and not args.no_serve:
@@ -396,7 +405,10 @@ def main():
         result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
     # ---- the other workloads: 512^2 twist frame; CPU samples of the rest ----
     if rank == 0 and world == 1 and not args.no_batch:
-        result["configs"] = bench_configs(eng, wl, predefined_source, pyoracle, cpu=not args.no_cpu)
+        result["configs"] = bench_configs(eng, wl, predefined_source, pyoracle, cpu=not args.no_cpu, keep=keep)
+    # ---- accuracy: every benchmarked workload against the FP64 oracle ----
+    if rank == 0 and not args.no_accuracy:
+        result["accuracy"] = accuracy_leg(keep)
     if rank == 0:
         print(json.dumps(result))
     eng.close()
@@ -404,9 +416,54 @@ def main():
         dist.destroy_process_group()
 
 
-def bench_lyapunov(eng, wl, predefined_source):
+def accuracy_leg(keep):
+    """The engine's results against the FP64 oracle (and the FP32 oracle's
+    own error beside them) on seeded pixel samples of every benchmarked
+    workload; oracle/accuracy.py defines each figure.  Runs after every timed
+    region, on the host cores."""
+    import torch
+    from linon_gb300 import _abi
+    from oracle import accuracy as acc
+    FIELD_NAMES = {_abi.FIELD_IDS[n]: n for n in ("linear", "twist", "lens", "lorenz_scaled")}
+    t0 = time.perf_counter()
+    out = {"endpoint_err_unit": "scene units (Euclidean distance to the FP64 oracle's endpoint)"}
+    if "frames_1080p" in keep:
+        w, pix, px = keep["frames_1080p"]
+        info = acc.FaceInfo(w.xyz, w.faces)
+        out["frames_1080p"] = {FIELD_NAMES[f]: acc.public(acc.frame_pixels_report(w, f, e, pix, info))
+                               for f, e in zip(w.fields, px)}
+        out["frames_1080p"]["sample"] = f"{len(pix)} pixels per field (seed 11) of the last timed frames"
+    if "plain_512_twist" in keep:
+        w, planes = keep["plain_512_twist"]
+        pix = acc.sample_pixels(w.width, w.height, 4000, seed=5)
+        out["plain_512_twist"] = acc.public(acc.frame_pixels_report(w, w.fields[0], planes.sample(pix), pix))
+        out["plain_512_twist"]["sample"] = "4000 pixels (seed 5)"
+    if "lyapunov_1024" in keep:
+        w, r = keep["lyapunov_1024"]
+        centres = acc.sample_pixels(w.width, w.height, 4000, seed=23, border=2)
+        idx = torch.as_tensor(centres.astype(np.int64), device=r["ftle"].device)
+        rep = acc.lyapunov_report(w, w.fields[0], centres, r["ftle"].reshape(-1)[idx].cpu().numpy(),
+                                  r["exponents"].reshape(-1)[idx].cpu().numpy(), r["threshold"],
+                                  r["outline_pixels"], w.extra["T"], engine_px=r["planes"].sample(centres),
+                                  info=acc.FaceInfo(w.xyz, w.faces))
+        out["lyapunov_1024"] = acc.public(rep)
+        out["lyapunov_1024"]["sample"] = "4000 interior pixels (seed 23), each with its 4 neighbours"
+    if "batch_uneven_64" in keep:
+        w, planes = keep["batch_uneven_64"]
+        views = w.extra["views"]
+        pix = [acc.sample_pixels(W, H, 200, seed=100 + i) for i, (W, H, *_r) in enumerate(views)]
+        eng = [p.sample(px) for p, px in zip(planes, pix)]
+        names = {i: FIELD_NAMES[f] for i, f in enumerate(w.fields)}
+        out["batch_uneven_64"] = acc.public(acc.batch_report(w, views, eng, pix, names))
+        out["batch_uneven_64"]["sample"] = "200 pixels per view (seeds 100..163), pooled per field"
+    out["oracle_s"] = time.perf_counter() - t0
+    return out
+
+
+def bench_lyapunov(eng, wl, predefined_source, keep=None):
     """Render + FP64 overlay + finite-time exponent (T = 4) + p95 threshold +
-    outline pixels + 8x100 outline capture, per-stage device ms (median of 3)."""
+    outline pixels + 8x100 outline capture, per-stage device ms (median of 3).
+    keep: receives the last run's maps for the accuracy leg."""
     import torch
     from linon_gb300 import lyapunov
     w = wl.lyapunov_1024()
@@ -417,6 +474,8 @@ def bench_lyapunov(eng, wl, predefined_source):
                 for _ in range(4)][1:]
     ms = {k: statistics.median(r["ms"][k] for r in runs) for k in runs[0]["ms"]}
     steps = int(runs[-1]["planes"].steps.sum().item())
+    if keep is not None:
+        keep["lyapunov_1024"] = (w, runs[-1])
     return {"workload": w.name, "ms": ms, "total_ms": sum(ms.values()),
             "render_ray_steps_per_s": steps / (ms["render"] * 1e-3), "threshold_p95": runs[-1]["threshold"]}
 
@@ -445,7 +504,7 @@ def bench_serving(eng, wl, predefined_source, seconds):
     return s
 
 
-def bench_batch(eng, stream, wl, torch, dev, predefined_source):
+def bench_batch(eng, stream, wl, torch, dev, predefined_source, keep=None):
     from linon_gb300 import FramePlanes, _abi
     w = wl.batch_uneven(64, seed=0)
     eng.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
@@ -485,6 +544,8 @@ def bench_batch(eng, stream, wl, torch, dev, predefined_source):
     eng.synchronize()
     steps_batch = sum(int(p.steps.sum().item()) for p in planes)
     rays = sum(v.width * v.height for v in views)
+    if keep is not None:  # the planes of the last (autotuned batched) render
+        keep["batch_uneven_64"] = (w, planes)
     return {"views": len(views), "rays": rays, "ray_steps": steps_batch, "plain_ms": plain_ms,
             "batched_ms": batch_ms, "plain_ray_steps_per_s": steps_plain / (plain_ms * 1e-3),
             "batched_ray_steps_per_s": steps_batch / (batch_ms * 1e-3), "speedup": plain_ms / batch_ms,

@@ -36,6 +36,18 @@ class FramePlanes:
                            torch.empty((height, width), dtype=torch.int32, device=device),
                            torch.empty((height, width), dtype=torch.int32, device=device))
 
+    def sample(self, pixels) -> dict:
+        """The planes at pixel indices row*W+x, gathered on the device and
+        copied to the host as numpy arrays."""
+        import torch
+        idx = torch.as_tensor(np.asarray(pixels, np.int64), device=self.mapping.device)
+        out = {}
+        for k in ("color", "mapping", "hit_id", "steps"):
+            t = getattr(self, k)
+            if t is not None:
+                out[k] = t.reshape(self.width * self.height, -1)[idx].squeeze(-1).cpu().numpy()
+        return out
+
     def abi(self) -> _abi.Frame:
         f = _abi.Frame()
         f.width, f.height = self.width, self.height

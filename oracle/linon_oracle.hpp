@@ -39,6 +39,7 @@
 //   * rgba8unorm stores round half to even after clamping to [0,1].
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -105,6 +106,123 @@ inline CountingFloat s_abs(CountingFloat x) { return CountingFloat(std::fabs(x.v
 inline CountingFloat s_min(CountingFloat a, CountingFloat b) { counts().cmp++; return CountingFloat(std::fmin(a.v, b.v)); }
 inline CountingFloat s_max(CountingFloat a, CountingFloat b) { counts().cmp++; return CountingFloat(std::fmax(a.v, b.v)); }
 
+// ---------------------------------------------------------------------------
+// TraceFloat: a float that records every operation on a tape, so that the
+// operations a ray's endpoint actually depends on can be counted (the
+// roofline's algorithmic work).  Rules:
+//   * liveness: the roots are the values the caller marks (the endpoint)
+//     and the operands of comparisons on loop-variant values (control
+//     flow); an operation is counted only if a root depends on it;
+//   * loop invariance: literals and march parameters are invariant, values
+//     marked by mark_carried (the state a step hands to the next) are not,
+//     and an operation on invariant operands only is invariant -- computed
+//     once per launch, not per step, so it is not counted;
+//   * launch constants: a product with an invariant 1 or 0, a sum with an
+//     invariant 0 and a quotient by an invariant 1 are not operations (the
+//     kernel variants specialise field_weight == 1; the rotation matrices'
+//     structural zeros and ones).
+// Negation and abs are free; min/max are comparisons, not FP32 arithmetic.
+// ---------------------------------------------------------------------------
+enum TraceKind : uint8_t { TK_LEAF, TK_ADD, TK_MUL, TK_DIV, TK_SQRT, TK_TRANSC, TK_FREE, TK_CMP };
+struct Tape {
+  std::vector<uint8_t> kind, inv;
+  std::vector<int32_t> a, b;
+  std::vector<int32_t> roots;
+  int32_t push(uint8_t k, int32_t x, int32_t y, bool invariant) {
+    kind.push_back(k);
+    inv.push_back(invariant ? 1 : 0);
+    a.push_back(x);
+    b.push_back(y);
+    return int32_t(kind.size() - 1);
+  }
+  void clear() { kind.clear(); inv.clear(); a.clear(); b.clear(); roots.clear(); }
+  // live, loop-variant operations by kind
+  void count(long long out[8]) const {
+    std::vector<uint8_t> live(kind.size(), 0);
+    for (int32_t r : roots) live[r] = 1;
+    for (int64_t i = int64_t(kind.size()) - 1; i >= 0; --i) {
+      if (!live[i]) continue;
+      if (a[i] >= 0) live[a[i]] = 1;
+      if (b[i] >= 0) live[b[i]] = 1;
+    }
+    for (int k = 0; k < 8; ++k) out[k] = 0;
+    for (size_t i = 0; i < kind.size(); ++i)
+      if (live[i] && !inv[i]) out[kind[i]]++;
+  }
+};
+inline Tape& tape() {
+  static thread_local Tape t;
+  return t;
+}
+
+struct TraceFloat {
+  float v;
+  int32_t id;
+  TraceFloat() : v(0.f), id(tape().push(TK_LEAF, -1, -1, true)) {}
+  TraceFloat(double x) : v(float(x)), id(tape().push(TK_LEAF, -1, -1, true)) {}
+  TraceFloat(float val, int32_t node, int) : v(val), id(node) {}
+  explicit operator float() const { return v; }
+};
+inline bool tr_inv(TraceFloat x) { return tape().inv[x.id] != 0; }
+inline bool tr_is(TraceFloat x, float c) { return tr_inv(x) && x.v == c; }
+inline TraceFloat tr_op(TraceKind k, TraceFloat x, TraceFloat y, float v) {
+  return TraceFloat(v, tape().push(k, x.id, y.id, tr_inv(x) && tr_inv(y)), 0);
+}
+inline TraceFloat tr_op1(TraceKind k, TraceFloat x, float v) {
+  return TraceFloat(v, tape().push(k, x.id, -1, tr_inv(x)), 0);
+}
+inline TraceFloat tr_const(float v) { return TraceFloat(v, tape().push(TK_LEAF, -1, -1, true), 0); }
+inline TraceFloat operator+(TraceFloat a, TraceFloat b) {
+  const float v = a.v + b.v;
+  if (tr_is(a, 0.0f)) return TraceFloat(v, b.id, 0);
+  if (tr_is(b, 0.0f)) return TraceFloat(v, a.id, 0);
+  return tr_op(TK_ADD, a, b, v);
+}
+inline TraceFloat operator-(TraceFloat a, TraceFloat b) {
+  const float v = a.v - b.v;
+  if (tr_is(b, 0.0f)) return TraceFloat(v, a.id, 0);
+  if (tr_is(a, 0.0f)) return tr_op1(TK_FREE, b, v);
+  return tr_op(TK_ADD, a, b, v);
+}
+inline TraceFloat operator*(TraceFloat a, TraceFloat b) {
+  const float v = a.v * b.v;
+  if (tr_is(a, 0.0f) || tr_is(b, 0.0f)) return tr_const(v);
+  if (tr_is(a, 1.0f)) return TraceFloat(v, b.id, 0);
+  if (tr_is(b, 1.0f)) return TraceFloat(v, a.id, 0);
+  return tr_op(TK_MUL, a, b, v);
+}
+inline TraceFloat operator/(TraceFloat a, TraceFloat b) {
+  const float v = a.v / b.v;
+  if (tr_is(b, 1.0f)) return TraceFloat(v, a.id, 0);
+  return tr_op(TK_DIV, a, b, v);
+}
+inline TraceFloat operator-(TraceFloat a) { return tr_op1(TK_FREE, a, -a.v); }
+inline void tr_control(TraceFloat a, TraceFloat b) {
+  if (!tr_inv(a)) tape().roots.push_back(a.id);
+  if (!tr_inv(b)) tape().roots.push_back(b.id);
+}
+inline bool operator<(TraceFloat a, TraceFloat b) { tr_control(a, b); return a.v < b.v; }
+inline bool operator>(TraceFloat a, TraceFloat b) { tr_control(a, b); return a.v > b.v; }
+inline bool operator<=(TraceFloat a, TraceFloat b) { tr_control(a, b); return a.v <= b.v; }
+inline bool operator>=(TraceFloat a, TraceFloat b) { tr_control(a, b); return a.v >= b.v; }
+inline bool operator==(TraceFloat a, TraceFloat b) { tr_control(a, b); return a.v == b.v; }
+inline TraceFloat& operator+=(TraceFloat& a, TraceFloat b) { a = a + b; return a; }
+inline TraceFloat s_sqrt(TraceFloat x) { return tr_op1(TK_SQRT, x, std::sqrt(x.v)); }
+inline TraceFloat s_sin(TraceFloat x) { return tr_op1(TK_TRANSC, x, std::sin(x.v)); }
+inline TraceFloat s_cos(TraceFloat x) { return tr_op1(TK_TRANSC, x, std::cos(x.v)); }
+inline TraceFloat s_exp(TraceFloat x) { return tr_op1(TK_TRANSC, x, std::exp(x.v)); }
+inline TraceFloat s_pow(TraceFloat x, TraceFloat y) { return tr_op(TK_TRANSC, x, y, std::pow(x.v, y.v)); }
+inline TraceFloat s_abs(TraceFloat x) { return tr_op1(TK_FREE, x, std::fabs(x.v)); }
+inline TraceFloat s_min(TraceFloat a, TraceFloat b) { return tr_op(TK_CMP, a, b, std::fmin(a.v, b.v)); }
+inline TraceFloat s_max(TraceFloat a, TraceFloat b) { return tr_op(TK_CMP, a, b, std::fmax(a.v, b.v)); }
+
+// Marks the state one march step hands to the next (loop-variant); a no-op
+// for the arithmetic scalars.
+inline void mark_carried(float&) {}
+inline void mark_carried(double&) {}
+inline void mark_carried(CountingFloat&) {}
+inline void mark_carried(TraceFloat& x) { x.id = tape().push(TK_FREE, x.id, -1, false); }
+
 template <class T> inline T lit(double x) { return T(x); }
 template <> inline float lit<float>(double x) { return float(x); }
 
@@ -135,6 +253,11 @@ template <class T> inline V3<T> normalize(V3<T> a) {
   return {a.x / l, a.y / l, a.z / l};
 }
 template <class T> inline V3<T> vabs(V3<T> a) { return {s_abs(a.x), s_abs(a.y), s_abs(a.z)}; }
+template <class T> inline void mark_carried(V3<T>& a) {
+  mark_carried(a.x);
+  mark_carried(a.y);
+  mark_carried(a.z);
+}
 // WGSL reflect(e1, e2) = e1 - 2 * dot(e2, e1) * e2
 template <class T> inline V3<T> reflect(V3<T> e1, V3<T> e2) {
   T d = lit<T>(2.0) * dot(e2, e1);
@@ -297,12 +420,92 @@ inline V3<T> field_eval(int id, V3<T> p_prev, V3<T> p, V3<T> v0, V3<T> v, T t) {
 // ---------------------------------------------------------------------------
 // Scene
 // ---------------------------------------------------------------------------
+// Candidate search for large scenes (the oracle's own, not the shader's):
+// a uniform grid over the triangles' bounding boxes, each inflated by a
+// margin far above any rounding of the Moeller-Trumbore quantities.  A
+// segment is tested against the triangles listed in the cells its inflated
+// box overlaps; since the closest hit is the lexicographic minimum of
+// (t, face index) -- the brute-force loop's strict `<` in face order -- the
+// order and repetition of candidates do not matter, and the result equals
+// the loop over all faces (held bit for bit by a CPU test).
+struct Accel {
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  double cell = 1.0, margin = 0.0;
+  int n[3] = {0, 0, 0};
+  std::vector<float> box;        // n_faces * 6 (inflated lo.xyz, hi.xyz)
+  std::vector<uint32_t> start;   // cells + 1
+  std::vector<uint32_t> items;   // face indices per cell
+};
+
 struct Scene {
   std::vector<float> xyz;      // n_vertices * 3
   std::vector<uint32_t> abc;   // n_faces * 3
   std::vector<float> face_rgb; // empty or n_faces * 3
+  const Accel* accel = nullptr;  // NULL: every face is tested (the shader's loop)
   uint32_t n_faces() const { return uint32_t(abc.size() / 3); }
 };
+
+// Builds the grid: `res` cells along the longest axis of the scene's box.
+inline void build_accel(const Scene& s, Accel& g, int res = 64) {
+  const uint32_t nf = s.n_faces();
+  g.box.assign(size_t(nf) * 6, 0.0f);
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (uint32_t i = 0; i < nf; ++i)
+    for (int k = 0; k < 3; ++k)
+      for (int c = 0; c < 3; ++c) {
+        const double x = s.xyz[3 * size_t(s.abc[3 * i + k]) + c];
+        lo[c] = std::fmin(lo[c], x);
+        hi[c] = std::fmax(hi[c], x);
+      }
+  double ext = 0.0;
+  for (int c = 0; c < 3; ++c) ext = std::fmax(ext, hi[c] - lo[c]);
+  if (!(ext > 0.0)) ext = 1.0;
+  g.margin = 1e-3 * ext + 1e-6;
+  for (uint32_t i = 0; i < nf; ++i)
+    for (int c = 0; c < 3; ++c) {
+      double a = 1e300, b = -1e300;
+      for (int k = 0; k < 3; ++k) {
+        const double x = s.xyz[3 * size_t(s.abc[3 * i + k]) + c];
+        a = std::fmin(a, x);
+        b = std::fmax(b, x);
+      }
+      g.box[6 * size_t(i) + c] = float(a - g.margin);
+      g.box[6 * size_t(i) + 3 + c] = float(b + g.margin);
+    }
+  for (int c = 0; c < 3; ++c) {
+    g.lo[c] = lo[c] - 2.0 * g.margin;
+    g.hi[c] = hi[c] + 2.0 * g.margin;
+  }
+  double gext = 0.0;
+  for (int c = 0; c < 3; ++c) gext = std::fmax(gext, g.hi[c] - g.lo[c]);
+  g.cell = gext / res;
+  for (int c = 0; c < 3; ++c) g.n[c] = std::max(1, int(std::ceil((g.hi[c] - g.lo[c]) / g.cell)));
+  const size_t ncell = size_t(g.n[0]) * g.n[1] * g.n[2];
+  std::vector<uint32_t> count(ncell + 1, 0);
+  auto range = [&](uint32_t i, int c, int& a, int& b) {
+    a = std::clamp(int(std::floor((double(g.box[6 * size_t(i) + c]) - g.lo[c]) / g.cell)), 0, g.n[c] - 1);
+    b = std::clamp(int(std::floor((double(g.box[6 * size_t(i) + 3 + c]) - g.lo[c]) / g.cell)), 0, g.n[c] - 1);
+  };
+  for (int pass = 0; pass < 2; ++pass) {
+    if (pass == 1) {
+      g.start.assign(ncell + 1, 0);
+      for (size_t c = 0; c < ncell; ++c) g.start[c + 1] = g.start[c] + count[c];
+      g.items.assign(g.start[ncell], 0);
+      std::fill(count.begin(), count.end(), 0);
+    }
+    for (uint32_t i = 0; i < nf; ++i) {
+      int a[3], b[3];
+      for (int c = 0; c < 3; ++c) range(i, c, a[c], b[c]);
+      for (int z = a[2]; z <= b[2]; ++z)
+        for (int y = a[1]; y <= b[1]; ++y)
+          for (int x = a[0]; x <= b[0]; ++x) {
+            const size_t cidx = (size_t(z) * g.n[1] + y) * g.n[0] + x;
+            if (pass == 1) g.items[g.start[cidx] + count[cidx]] = i;
+            count[cidx]++;
+          }
+    }
+  }
+}
 
 template <class T> inline V3<T> vertex(const Scene& s, uint32_t i) {
   return V3<T>(lit<T>(s.xyz[3 * i]), lit<T>(s.xyz[3 * i + 1]), lit<T>(s.xyz[3 * i + 2]));
@@ -336,23 +539,78 @@ template <class T> struct ColorHit {
 
 // ray_color, main_view.wgsl:177-220.  Closest hit over all faces with strict
 // `<`, so ties keep the lower face index.
+template <class T> inline double to_double(T x) { return double(x); }
+template <> inline double to_double<CountingFloat>(CountingFloat x) { return double(x.v); }
+template <> inline double to_double<TraceFloat>(TraceFloat x) { return double(x.v); }
+
+// Candidate faces of a segment from the grid; false when the grid does not
+// apply (no grid, non-finite segment, or a segment spanning more cells than
+// there are faces), and the caller tests every face.
+template <class T>
+inline bool grid_candidates(const Scene& sc, V3<T> origin, V3<T> direction, T max_dist,
+                            std::vector<uint32_t>& out) {
+  const Accel* g = sc.accel;
+  if (!g) return false;
+  const double o[3] = {to_double(origin.x), to_double(origin.y), to_double(origin.z)};
+  const double d[3] = {to_double(direction.x), to_double(direction.y), to_double(direction.z)};
+  const double L = to_double(max_dist);
+  double smin[3], smax[3];
+  for (int c = 0; c < 3; ++c) {
+    if (!std::isfinite(o[c]) || !std::isfinite(d[c]) || !std::isfinite(L)) return false;
+    const double e = o[c] + d[c] * L;
+    smin[c] = std::fmin(o[c], e) - g->margin;
+    smax[c] = std::fmax(o[c], e) + g->margin;
+  }
+  out.clear();
+  int a[3], b[3];
+  for (int c = 0; c < 3; ++c) {
+    if (smax[c] < g->lo[c] || smin[c] > g->hi[c]) return true;  // outside every face's box
+    a[c] = std::clamp(int(std::floor((smin[c] - g->lo[c]) / g->cell)), 0, g->n[c] - 1);
+    b[c] = std::clamp(int(std::floor((smax[c] - g->lo[c]) / g->cell)), 0, g->n[c] - 1);
+  }
+  const double cells = double(b[0] - a[0] + 1) * (b[1] - a[1] + 1) * (b[2] - a[2] + 1);
+  if (cells > double(sc.n_faces())) return false;
+  for (int z = a[2]; z <= b[2]; ++z)
+    for (int y = a[1]; y <= b[1]; ++y)
+      for (int x = a[0]; x <= b[0]; ++x) {
+        const size_t cidx = (size_t(z) * g->n[1] + y) * g->n[0] + x;
+        for (uint32_t k = g->start[cidx]; k < g->start[cidx + 1]; ++k) {
+          const uint32_t i = g->items[k];
+          const float* bx = &g->box[6 * size_t(i)];
+          if (smax[0] < bx[0] || smin[0] > bx[3] || smax[1] < bx[1] || smin[1] > bx[4] ||
+              smax[2] < bx[2] || smin[2] > bx[5])
+            continue;
+          out.push_back(i);
+        }
+      }
+  return true;
+}
+
 template <class T>
 inline ColorHit<T> ray_color(const Scene& sc, V3<T> origin, V3<T> direction, T max_dist) {
   T t = lit<T>(-1.0);
   V3<T> d1, d2;
   int32_t face = -1;
   const uint32_t nf = sc.n_faces();
-  for (uint32_t i = 0; i < nf; ++i) {
+  auto test = [&](uint32_t i) {
     V3<T> a = vertex<T>(sc, sc.abc[3 * i]);
     V3<T> b = vertex<T>(sc, sc.abc[3 * i + 1]);
     V3<T> c = vertex<T>(sc, sc.abc[3 * i + 2]);
     T t_new = hit_triangle(a, b, c, origin, direction);
-    if (t_new > lit<T>(0.0) && t_new < max_dist && (t < lit<T>(0.0) || t_new < t)) {
+    // strict `<` in face order == lexicographic minimum of (t, face)
+    if (t_new > lit<T>(0.0) && t_new < max_dist &&
+        (t < lit<T>(0.0) || t_new < t || (!(t < t_new) && int32_t(i) < face))) {
       t = t_new;
       d1 = b - a;
       d2 = c - a;
       face = int32_t(i);
     }
+  };
+  static thread_local std::vector<uint32_t> cand;
+  if (grid_candidates(sc, origin, direction, max_dist, cand)) {
+    for (uint32_t i : cand) test(i);
+  } else {
+    for (uint32_t i = 0; i < nf; ++i) test(i);
   }
   ColorHit<T> r;
   if (t > lit<T>(0.0) && t < max_dist) {
@@ -435,6 +693,17 @@ inline RayResult<T> nonlinear_ray_color(const Scene& sc, int field, V3<T> start_
   const T half = lit<T>(0.5), two = lit<T>(2.0), six = lit<T>(6.0), ten = lit<T>(10.0);
 
   for (;;) {
+    // the state this step receives from the previous one (for TraceFloat)
+    mark_carried(cur_point);
+    mark_carried(cur_dir);
+    mark_carried(t);
+    mark_carried(comp_p);
+    mark_carried(comp_t);
+    if (m.adaptive) {  // otherwise h stays h_initial and these are unused
+      mark_carried(h);
+      mark_carried(last_v);
+      mark_carried(last_diff);
+    }
     if (m.max_steps > 0) {
       if (steps >= m.max_steps) break;
     } else {
@@ -470,7 +739,9 @@ inline RayResult<T> nonlinear_ray_color(const Scene& sc, int field, V3<T> start_
       t = t + h;
     }
     last_v = v;
-    if (two * diff < last_diff && h < h_initial) h = h_initial;
+    // (h only leaves h_initial through the adaptive refinement above, so the
+    // restore needs m.adaptive; the guard changes no result)
+    if (m.adaptive && two * diff < last_diff && h < h_initial) h = h_initial;
     last_diff = diff;
     steps++;
     if (m.stop_on_hit && has_color) break;

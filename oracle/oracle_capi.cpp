@@ -93,14 +93,22 @@ extern "C" {
 
 // Renders a frame (pixels == NULL) or the listed pixels (indices row*W+x,
 // outputs compacted in list order).  precision: 32 or 64.
+// accel != 0 tests each segment against the faces the oracle's candidate
+// grid lists (the same result as the loop over all faces, faster on large
+// scenes); accel == 0 is the shader's loop.
 int oracle_render(int precision, const float* xyz, int nv, const uint32_t* abc, int nf,
                   const float* face_rgb, const linon_camera* cam, const linon_settings* st,
                   const linon_march_params* mp, int field, int W, int H, const int32_t* pixels,
                   int64_t npix, uint8_t* color, float* mapping, double* mapping64, int32_t* hit,
-                  int32_t* steps, int nthreads) {
+                  int32_t* steps, int nthreads, int accel) {
   if (!xyz || !abc || !cam || !mp || W <= 0 || H <= 0) return LINON_EINVAL;
   if (nthreads <= 0) nthreads = omp_get_max_threads();
   Scene sc = make_scene(xyz, nv, abc, nf, face_rgb);
+  Accel grid;
+  if (accel) {
+    build_accel(sc, grid);
+    sc.accel = &grid;
+  }
   March m = make_march(st, mp);
   Camera c = make_camera(cam);
   if (precision == 64)
@@ -132,6 +140,43 @@ int oracle_count_ops(const float* xyz, int nv, const uint32_t* abc, int nf,
     out[6 * i + 3] = k.sqrt; out[6 * i + 4] = k.cmp; out[6 * i + 5] = k.transc;
     steps_out[i] = r.steps;
   }
+  return LINON_OK;
+}
+
+// Algorithmic FP32 operations per accepted step (TraceFloat): the operations
+// the ray's endpoint depends on, loop-invariant work and launch-constant
+// products excluded.  Per listed pixel, the live loop-variant operations of
+// a march of `steps_a` and of `steps_b` (> steps_a) fixed steps on the given
+// scene are taken and their difference divided by steps_b - steps_a, so the
+// work before the first and after the last step cancels.  out[i*8 + k],
+// k = add, mul, div, sqrt, transcendental, free, cmp (TraceKind order from 1).
+int oracle_count_live_ops(const float* xyz, int nv, const uint32_t* abc, int nf,
+                          const linon_camera* cam, const linon_settings* st,
+                          const linon_march_params* mp, int field, int W, int H,
+                          const int32_t* pixels, int npix, int steps_a, int steps_b, double* out) {
+  if (steps_b <= steps_a || steps_a <= 0 || mp->adaptive) return LINON_EINVAL;
+  Scene sc = make_scene(xyz, nv, abc, nf, nullptr);
+  Camera c = make_camera(cam);
+  for (int i = 0; i < npix; ++i) {
+    int row = pixels[i] / W, x = pixels[i] % W;
+    long long cnt[2][8];
+    for (int pass = 0; pass < 2; ++pass) {
+      March m = make_march(st, mp);
+      m.max_steps = pass == 0 ? steps_a : steps_b;
+      m.stop_on_hit = false;
+      tape().clear();
+      CameraBasis<TraceFloat> b = camera_basis<TraceFloat>(c, W, H, m);
+      RayResult<TraceFloat> r = render_pixel<TraceFloat>(sc, field, b, W, H, x, row, m);
+      tape().roots.push_back(r.mapping.x.id);
+      tape().roots.push_back(r.mapping.y.id);
+      tape().roots.push_back(r.mapping.z.id);
+      tape().count(cnt[pass]);
+    }
+    for (int k = 0; k < 7; ++k)
+      out[8 * i + k] = double(cnt[1][k + 1] - cnt[0][k + 1]) / double(steps_b - steps_a);
+    out[8 * i + 7] = 0.0;
+  }
+  tape().clear();
   return LINON_OK;
 }
 
@@ -184,6 +229,21 @@ int oracle_primary_dirs(const linon_camera* cam, const linon_march_params* mp, i
   for (int i = 0; i < npix; ++i) {
     int row = pixels[i] / W, x = pixels[i] % W;
     V3<float> d = primary_dir(b, x, H - 1 - row);
+    out[3 * i] = d.x; out[3 * i + 1] = d.y; out[3 * i + 2] = d.z;
+  }
+  return LINON_OK;
+}
+
+// The same directions in FP64 (the camera basis and the normalisation in
+// double), for the FP64 finite-time exponent.
+int oracle_primary_dirs64(const linon_camera* cam, const linon_march_params* mp, int W, int H,
+                          const int32_t* pixels, int npix, double* out) {
+  March m = make_march(nullptr, mp);
+  Camera c = make_camera(cam);
+  CameraBasis<double> b = camera_basis<double>(c, W, H, m);
+  for (int i = 0; i < npix; ++i) {
+    int row = pixels[i] / W, x = pixels[i] % W;
+    V3<double> d = primary_dir(b, x, H - 1 - row);
     out[3 * i] = d.x; out[3 * i + 1] = d.y; out[3 * i + 2] = d.z;
   }
   return LINON_OK;

@@ -35,14 +35,17 @@ def lib():
         _lib = C.CDLL(str(LIB))
         vp = C.c_void_p
         _lib.oracle_render.argtypes = [C.c_int, vp, C.c_int, vp, C.c_int, vp, vp, vp, vp, C.c_int, C.c_int,
-                                       C.c_int, vp, C.c_int64, vp, vp, vp, vp, vp, C.c_int]
+                                       C.c_int, vp, C.c_int64, vp, vp, vp, vp, vp, C.c_int, C.c_int]
         _lib.oracle_count_ops.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp, vp, C.c_int, C.c_int, C.c_int,
                                           vp, C.c_int, vp, vp]
         _lib.oracle_count_field.argtypes = [C.c_int, vp, vp]
+        _lib.oracle_count_live_ops.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp, vp, C.c_int, C.c_int, C.c_int,
+                                               vp, C.c_int, C.c_int, C.c_int, vp]
         _lib.oracle_field_eval.argtypes = [C.c_int, C.c_int, vp, C.c_int64, vp, vp]
         _lib.oracle_hit_triangle.argtypes = [vp, vp]
         _lib.oracle_hit_triangle.restype = C.c_float
         _lib.oracle_primary_dirs.argtypes = [vp, vp, C.c_int, C.c_int, vp, C.c_int, vp]
+        _lib.oracle_primary_dirs64.argtypes = [vp, vp, C.c_int, C.c_int, vp, C.c_int, vp]
         _lib.oracle_overlay.argtypes = [C.c_int, vp, vp, C.c_int, C.c_int, vp, C.c_int, vp, vp, C.c_int]
         _lib.oracle_ftle.argtypes = [vp, vp, C.c_int, C.c_int, vp, C.c_double, vp]
         _lib.oracle_capture.argtypes = [C.c_int, C.c_int, vp, vp, vp, C.c_int, C.c_int, vp, C.c_int, C.c_float,
@@ -56,8 +59,10 @@ def _p(a):
 
 
 def render(xyz, faces, face_rgb, camera, settings, params, field_id, width, height, pixels=None,
-           precision=32, threads=0, want=("color", "mapping", "hit_id", "steps")):
-    """Renders the frame (or the listed pixel indices row*W+x) on the CPU."""
+           precision=32, threads=0, want=("color", "mapping", "hit_id", "steps"), accel=False):
+    """Renders the frame (or the listed pixel indices row*W+x) on the CPU.
+    accel: test each segment against the faces listed by the oracle's
+    candidate grid instead of every face (equal results; for large scenes)."""
     xyz = np.ascontiguousarray(xyz, np.float32)
     faces = np.ascontiguousarray(faces, np.uint32)
     rgb = None if face_rgb is None else np.ascontiguousarray(face_rgb, np.float32)
@@ -77,7 +82,8 @@ def render(xyz, faces, face_rgb, camera, settings, params, field_id, width, heig
     st = lib().oracle_render(precision, _p(xyz), len(xyz), _p(faces), len(faces), _p(rgb), C.addressof(camera),
                              C.addressof(settings), C.addressof(params), field_id, width, height, _p(pix),
                              0 if pix is None else len(pix), _p(out.get("color")), _p(out.get("mapping")),
-                             _p(out.get("mapping64")), _p(out.get("hit_id")), _p(out.get("steps")), threads)
+                             _p(out.get("mapping64")), _p(out.get("hit_id")), _p(out.get("steps")), threads,
+                             1 if accel else 0)
     assert st == 0
     if pixels is None:
         for k, v in list(out.items()):
@@ -94,6 +100,23 @@ def count_ops(xyz, faces, camera, settings, params, field_id, width, height, pix
     lib().oracle_count_ops(_p(xyz), len(xyz), _p(faces), len(faces), C.addressof(camera), C.addressof(settings),
                            C.addressof(params), field_id, width, height, _p(pix), len(pix), _p(out), _p(steps))
     return out, steps
+
+
+def count_live_ops(xyz, faces, camera, settings, params, field_id, width, height, pixels, steps_a=64,
+                   steps_b=128):
+    """Algorithmic FP32 operations per accepted step at each listed pixel:
+    the operations the endpoint depends on, without loop-invariant work or
+    products by launch constants (oracle_count_live_ops).  Returns a float
+    array [n, 7]: add, mul, div, sqrt, transcendental, free, cmp."""
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    faces = np.ascontiguousarray(faces, np.uint32)
+    pix = np.ascontiguousarray(pixels, np.int32)
+    out = np.zeros((len(pix), 8), np.float64)
+    st = lib().oracle_count_live_ops(_p(xyz), len(xyz), _p(faces), len(faces), C.addressof(camera),
+                                     C.addressof(settings), C.addressof(params), field_id, width, height, _p(pix),
+                                     len(pix), steps_a, steps_b, _p(out))
+    assert st == 0, st
+    return out[:, :7]
 
 
 def count_field(field_id, inputs13):
@@ -120,8 +143,13 @@ def hit_triangle(tri9, ray6) -> float:
     return float(lib().oracle_hit_triangle(_p(a), _p(b)))
 
 
-def primary_dirs(camera, params, width, height, pixels):
+def primary_dirs(camera, params, width, height, pixels, precision=32):
     pix = np.ascontiguousarray(pixels, np.int32)
+    if precision == 64:
+        out = np.zeros((len(pix), 3), np.float64)
+        lib().oracle_primary_dirs64(C.addressof(camera), C.addressof(params), width, height, _p(pix), len(pix),
+                                    _p(out))
+        return out
     out = np.zeros((len(pix), 3), np.float32)
     lib().oracle_primary_dirs(C.addressof(camera), C.addressof(params), width, height, _p(pix), len(pix), _p(out))
     return out

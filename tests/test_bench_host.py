@@ -43,3 +43,23 @@ def test_cpu_samplers():
     v, threads, sample = bench.cpu_views_sample(pyoracle, views, w, budget_s=0.05)
     assert v > 0 and "rays" in sample and "views" in sample
     assert np.isfinite(v)
+
+
+def test_flops_per_step_counts_live_operations():
+    """The roofline's numerator: operations the endpoint depends on, per
+    ray-step of the 1080p workload (h = 0.005, Kahan sums, field_weight 1).
+    linear: f = v0 is loop-invariant, so only the Kahan sum of the position
+    remains (4 operations x 3 components); twist: the y components of the
+    field and of the stage positions are invariant; lens: every component
+    is live; all below the count of every operation the oracle performs."""
+    w = wl.frames_1080p()
+    got = {name: bench.flops_per_step(pyoracle, w, wl._abi.FIELD_IDS[name]) for name in ("linear", "twist", "lens")}
+    assert got["linear"] == (12.0, 0.0)
+    assert got["twist"] == (57.0, 8.0)
+    assert got["lens"] == (147.0, 4.0)
+    e, f = np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32)
+    pix = np.array([w.width // 2 + (w.height // 2) * w.width], np.int32)
+    for name, (live, _) in got.items():
+        ops, steps = pyoracle.count_ops(e, f, w.camera, w.settings, wl.fixed_steps(0.005, 64, kahan=True),
+                                        wl._abi.FIELD_IDS[name], w.width, w.height, pix)
+        assert live < ops[0, :4].sum() / steps[0]
