@@ -11,12 +11,13 @@ error on the same pixels beside it.  Tolerances, stated per test:
     RGBA8 within 1/255 on pixels whose hit ids agree;
   * the point-lens field, whose orbits around the origin are chaotic (the
     FP32 oracle itself is 5e-3 from FP64 at the median): equal accuracy --
-    the engine's p50 / p90 / p99 endpoint error at most 1.25x the FP32
-    oracle's on the same pixels -- and hit mismatch outside ties no more
-    than the FP32 oracle's plus 0.1%;
+    each of the engine's p50 / p90 / p99 endpoint errors within 1e-4 or at
+    most 1.25x the FP32 oracle's on the same pixels -- and hit mismatch
+    outside ties no more than the FP32 oracle's plus 0.1%;
   * Lyapunov: finite-time exponent and scaled overlay exponent from FP64
-    endpoints of each sampled pixel and its four neighbours; the p95
-    threshold on the sample within 1e-3 of the FP64 one.
+    endpoints of each sampled pixel and its four neighbours (the exponent
+    within 1e-4 absolute, or no worse than 1.25x the FP32 oracle's error);
+    the p95 threshold on the sample within 1e-3 of the FP64 one.
 """
 import numpy as np
 import pytest
@@ -98,9 +99,9 @@ def test_lyapunov_1024_fast_vs_fp64(engine, acc):
     rep = acc.lyapunov_report(w, fid, centres, e_ftle, e_expo, r["threshold"], r["outline_pixels"], w.extra["T"],
                               engine_px=r["planes"].sample(centres), info=acc.FaceInfo(w.xyz, w.faces))
     _check_frame(rep["frame"], "lorenz_scaled")
-    ft, ft32 = rep["ftle_abs_err"], rep["ftle_abs_err_fp32_oracle"]
-    for q in ("p50", "p90", "p99"):
-        assert ft[q] <= 1.25 * ft32[q] + 1e-6, (q, ft, ft32)
+    # finite-time exponent: within 1e-4 (absolute) at every quantile, or no
+    # worse than 1.25x the FP32 oracle's own error
+    assert rep["ftle_equal_accuracy"]["ok"], (rep["ftle_abs_err"], rep["ftle_abs_err_fp32_oracle"])
     assert rep["p95_on_sample"]["abs_diff"] <= 1e-3, rep["p95_on_sample"]
     assert rep["above_p95_agree"] >= 0.995, rep["above_p95_agree"]
     assert rep["overlay_exponent_rel_err"]["p99"] <= 1e-3, rep["overlay_exponent_rel_err"]

@@ -113,7 +113,12 @@ def test_lyapunov_report_of_the_fp32_oracle(oracle, acc):
                           precision=64)
     centres = acc.sample_pixels(w.width, w.height, 500, seed=2, border=2)
     thr = float(np.quantile(f[1:-1, 1:-1], 0.95))
-    rep = acc.lyapunov_report(w, fid, centres, f.ravel()[centres], e.ravel()[centres], thr, None, 3.0)
+    outline = oracle.outline_select(f, w.width, w.height, thr)
+    rep = acc.lyapunov_report(w, fid, centres, f.ravel()[centres], e.ravel()[centres], thr, outline, 3.0)
+    # the outline pixels (extremal pixels above the threshold, image borders
+    # included) are above it under the FP64 exponent too
+    assert rep["outline_pixels_checked"] >= 1
+    assert rep["outline_pixels_above_engine_threshold_in_fp64"] >= rep["outline_pixels_checked"] - 1
     # the FP32 oracle's own maps: the finite-time exponent is the FP32
     # pipeline's (FP32 directions), so its error equals the FP32 column
     assert rep["ftle_abs_err"]["max"] <= rep["ftle_abs_err_fp32_oracle"]["max"] * 1.0001 + 1e-6
