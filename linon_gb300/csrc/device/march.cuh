@@ -434,7 +434,7 @@ struct RayState {
   float h, last_diff;
   wgsl::vec4f color;
   vec3f q0;             // centre of the current safe ball
-  float safe2;          // its squared radius (< 0: no ball)
+  float safe2;          // its squared radius (< 0: no ball; +inf: hit, no more tests)
   int face;
   int steps;
   int cool;             // steps left before the next safe-distance query
@@ -537,29 +537,35 @@ __device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevM
     r.dir = wgsl::vmadd(v, w, (1.0f - w) * r.dir);
   }
   const vec3f step_dir = wgsl::vscale(r.dir, h);
-  if (!r.has_color) {
-    // Safe-ball skip (BVH scenes): every point within the ball of radius
-    // sqrt(safe2) around q0 is farther than the culling margin from every
-    // triangle, and a segment whose ends both lie in the ball lies in it
-    // (the ball is convex; the start was checked by the previous step), so
-    // such a segment cannot hit anything the brute-force loop would hit.
-    const vec3f seg_end = wgsl::vadd(r.p, step_dir);
-    const vec3f dq = wgsl::vsub(seg_end, r.q0);
-    if (!(sc.n_nodes > 0 && wgsl::dot(dq, dq) <= r.safe2)) {
-      const float len = wgsl::length(step_dir);
+  // Safe-ball skip: every point within the ball of radius sqrt(safe2) around
+  // q0 is farther than the culling margin from every triangle, and a
+  // segment whose ends both lie in the ball lies in it (the ball is convex;
+  // the start was checked by the previous step), so such a segment cannot
+  // hit anything the brute-force loop would hit.  safe2 also encodes the
+  // two other cases, so that the step takes one test on its common path:
+  // +inf once the ray has its first hit (nothing is tested after it), -1 on
+  // scenes without a BVH (every segment is tested).  A NaN distance fails
+  // the test, as a segment leaving the ball does.
+  const vec3f seg_end = wgsl::vadd(r.p, step_dir);
+  const vec3f dq = wgsl::vsub(seg_end, r.q0);
+  if (!(wgsl::dot(dq, dq) <= r.safe2) && !r.has_color) {
+    const float len = wgsl::length(step_dir);
 #if defined(LINON_PRECISE)
-      const vec3f dirn = step_dir / len;
+    const vec3f dirn = step_dir / len;
 #else
-      const vec3f dirn = wgsl::normalize(step_dir);
+    const vec3f dirn = wgsl::normalize(step_dir);
 #endif
-      HitRec hit = intersect_segment_cells<PAIR>(sc, r.p, dirn, len, seg_end, err);
-      if (hit.t > 0.0f && hit.t < len) {
-        r.color = shade_hit(sc, hit, dirn);
-        r.has_color = r.color.w > 0.0f;
-        if (r.has_color) r.face = hit.id;
-      }
+    HitRec hit = intersect_segment_cells<PAIR>(sc, r.p, dirn, len, seg_end, err);
+    if (hit.t > 0.0f && hit.t < len) {
+      r.color = shade_hit(sc, hit, dirn);
+      r.has_color = r.color.w > 0.0f;
+      if (r.has_color) r.face = hit.id;
+    }
+    if (r.has_color) {
+      r.safe2 = __int_as_float(0x7f800000);  // +inf: no more tests
+    } else {
       r.safe2 = -1.0f;
-      if (!r.has_color && sc.n_nodes > 0) {
+      if (sc.n_nodes > 0) {
         if (r.cool > 0) {
           r.cool--;
         } else {

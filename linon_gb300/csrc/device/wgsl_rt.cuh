@@ -26,9 +26,23 @@ namespace wgsl {
 // ---------------------------------------------------------------------------
 // scalar math
 // ---------------------------------------------------------------------------
+// Reciprocal square root of fast modules: the special-function unit's
+// approximation with a subnormal argument flushed to zero (result +inf).
+// rsqrtf keeps subnormal arguments exact by scaling them, which costs a
+// compare and two predicated multiplies around every call; the only inputs
+// that need it are squared lengths below 2^-126 (vectors shorter than
+// 1.1e-19), whose normalisation then gives inf or NaN instead of a unit
+// vector.
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+#endif
 WG_HD float rsqrt_(float x) {
 #if defined(__CUDA_ARCH__) && !defined(LINON_PRECISE)
-  return rsqrtf(x);
+  return rsqrt_ftz(x);
 #else
   return 1.0f / sqrtf(x);
 #endif
@@ -150,9 +164,9 @@ WG_HD float pow_k(float x, float k) {
   if (k == 4.0f) { const float y = x * x; return y * y; }
   if (k == 0.5f) return sqrtf(x);
   if (k == 1.5f) return x * sqrtf(x);
-  if (k == -0.5f) return rsqrtf(x);
+  if (k == -0.5f) return rsqrt_ftz(x);
   if (k == -1.0f) return 1.0f / x;
-  if (k == -1.5f) { const float r = rsqrtf(x); return r * r * r; }
+  if (k == -1.5f) { const float r = rsqrt_ftz(x); return r * r * r; }
   if (k == -2.0f) { const float r = 1.0f / x; return r * r; }
   if (k == -3.0f) { const float r = 1.0f / x; return r * r * r; }
 #endif
@@ -241,7 +255,7 @@ struct arr {
 WG_HD float scaled_pow_neg_k(float s, float x, float k) {
 #if !defined(LINON_PRECISE) && defined(__CUDA_ARCH__)
   if (k == 1.5f) {
-    const float r = rsqrtf(x);
+    const float r = rsqrt_ftz(x);
     return (s * r) * (r * r);
   }
 #endif
@@ -737,16 +751,13 @@ WG_HD vec3f vadd(const vec3f& a, const vec3f& b) {
   return a + b;
 #endif
 }
-// a - b (PTX sub.rn.f32x2; there is no packed-subtract builtin)
+// a - b, as a + (-b): there is no packed-subtract builtin, and the
+// negation is an operand modifier of the packed add (exact, so the result
+// rounds like the subtraction)
 WG_HD vec3f vsub(const vec3f& a, const vec3f& b) {
 #ifdef LINON_F32X2
-  unsigned long long pa, pb, pd;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(pa) : "f"(a.x), "f"(a.y));
-  asm("mov.b64 %0, {%1, %2};" : "=l"(pb) : "f"(b.x), "f"(b.y));
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(pd) : "l"(pa), "l"(pb));
-  float rx, ry;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(rx), "=f"(ry) : "l"(pd));
-  return vec3f(rx, ry, a.z - b.z);
+  const float2 r = __fadd2_rn(xy2(a), make_float2(-b.x, -b.y));
+  return vec3f(r.x, r.y, a.z - b.z);
 #else
   return a - b;
 #endif
@@ -757,7 +768,7 @@ template <int N> WG_HD vec<float, N> normalize(const vec<float, N>& v) {
   float l = sqrtf(dot(v, v));
   return v / l;
 #else
-  return v * rsqrtf(dot(v, v));
+  return v * rsqrt_ftz(dot(v, v));
 #endif
 }
 // LINON_PACKED_NORMALIZE: fast float3 normalize scales x/y as one packed
@@ -765,7 +776,7 @@ template <int N> WG_HD vec<float, N> normalize(const vec<float, N>& v) {
 // on the kernel's register allocation, so the module that includes this
 // file decides).
 #if defined(LINON_F32X2) && defined(LINON_PACKED_NORMALIZE)
-template <> WG_HD vec3f normalize<3>(const vec3f& v) { return vscale(v, rsqrtf(dot(v, v))); }
+template <> WG_HD vec3f normalize<3>(const vec3f& v) { return vscale(v, rsqrt_ftz(dot(v, v))); }
 #endif
 // reflect(e1, e2) = e1 - 2 * dot(e2, e1) * e2
 template <int N> WG_HD vec<float, N> reflect(const vec<float, N>& e1, const vec<float, N>& e2) {
