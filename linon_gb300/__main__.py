@@ -73,7 +73,7 @@ def cmd_batch(a):
         if a.plain:
             eng.render_views_plain(flds, views)
         elif a.schedule == 1:
-            eng.render_batch(flds, views, _abi.BatchTuning(a.quantum, 128, 0, 4, 8, 0, 1))
+            eng.render_batch(flds, views, _abi.BatchTuning(a.quantum, a.block_threads, 0, 4, 8, a.refill_below, 1))
         elif a.schedule == 2:
             eng.render_batch(flds, views, _abi.BatchTuning(0, 0, 0, 0, 0, 0, 2))
         else:
@@ -83,7 +83,8 @@ def cmd_batch(a):
         e.synchronize()
         ts.append(s.elapsed_time(e))
     steps = sum(int(p.steps.sum().item()) for p in planes)
-    print(json.dumps({"views": len(views), "plain": a.plain, "schedule": a.schedule, "ms": ts, "ray_steps": steps,
+    print(json.dumps({"views": len(views), "plain": a.plain, "schedule": a.schedule, "quantum": a.quantum,
+                      "refill_below": a.refill_below, "block_threads": a.block_threads, "ms": ts, "ray_steps": steps,
                       "ray_steps_per_s": steps / (statistics.median(ts) * 1e-3)}))
     eng.close()
 
@@ -111,6 +112,9 @@ def main():
     b.add_argument("--schedule", type=int, default=0, choices=(0, 1, 2),
                    help="0 the default (one CTA per tile), 1 persistent work queue, 2 one CTA per tile")
     b.add_argument("--quantum", type=int, default=1024, help="RK4 steps per quantum (persistent queue)")
+    b.add_argument("--refill-below", type=int, default=0,
+                   help="persistent queue: refill a warp's free lanes once fewer than this many are marching")
+    b.add_argument("--block-threads", type=int, default=128, help="persistent queue: threads per CTA")
     v = sub.add_parser("validate")
     v.add_argument("--field", default="twist")
     v.add_argument("--precise", action="store_true")

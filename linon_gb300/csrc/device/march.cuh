@@ -434,7 +434,7 @@ struct RayState {
   float h, last_diff;
   wgsl::vec4f color;
   vec3f q0;             // centre of the current safe ball
-  float safe2;          // its squared radius (< 0: no ball; +inf: hit, no more tests)
+  float safe2;          // its squared radius (< 0: no ball)
   int face;
   int steps;
   int cool;             // steps left before the next safe-distance query
@@ -541,31 +541,29 @@ __device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevM
   // q0 is farther than the culling margin from every triangle, and a
   // segment whose ends both lie in the ball lies in it (the ball is convex;
   // the start was checked by the previous step), so such a segment cannot
-  // hit anything the brute-force loop would hit.  safe2 also encodes the
-  // two other cases, so that the step takes one test on its common path:
-  // +inf once the ray has its first hit (nothing is tested after it), -1 on
-  // scenes without a BVH (every segment is tested).  A NaN distance fails
-  // the test, as a segment leaving the ball does.
-  const vec3f seg_end = wgsl::vadd(r.p, step_dir);
-  const vec3f dq = wgsl::vsub(seg_end, r.q0);
-  if (!(wgsl::dot(dq, dq) <= r.safe2) && !r.has_color) {
-    const float len = wgsl::length(step_dir);
+  // hit anything the brute-force loop would hit.  After the first hit
+  // nothing is tested; before it, safe2 = -1 on scenes without a BVH makes
+  // every segment fail the one test (no scene constant is read on this
+  // path), and a NaN distance fails it too, as a segment leaving the ball
+  // does.
+  if (!r.has_color) {
+    const vec3f seg_end = wgsl::vadd(r.p, step_dir);
+    const vec3f dq = wgsl::vsub(seg_end, r.q0);
+    if (!(wgsl::dot(dq, dq) <= r.safe2)) {
+      const float len = wgsl::length(step_dir);
 #if defined(LINON_PRECISE)
-    const vec3f dirn = step_dir / len;
+      const vec3f dirn = step_dir / len;
 #else
-    const vec3f dirn = wgsl::normalize(step_dir);
+      const vec3f dirn = wgsl::normalize(step_dir);
 #endif
-    HitRec hit = intersect_segment_cells<PAIR>(sc, r.p, dirn, len, seg_end, err);
-    if (hit.t > 0.0f && hit.t < len) {
-      r.color = shade_hit(sc, hit, dirn);
-      r.has_color = r.color.w > 0.0f;
-      if (r.has_color) r.face = hit.id;
-    }
-    if (r.has_color) {
-      r.safe2 = __int_as_float(0x7f800000);  // +inf: no more tests
-    } else {
+      HitRec hit = intersect_segment_cells<PAIR>(sc, r.p, dirn, len, seg_end, err);
+      if (hit.t > 0.0f && hit.t < len) {
+        r.color = shade_hit(sc, hit, dirn);
+        r.has_color = r.color.w > 0.0f;
+        if (r.has_color) r.face = hit.id;
+      }
       r.safe2 = -1.0f;
-      if (sc.n_nodes > 0) {
+      if (!r.has_color && sc.n_nodes > 0) {
         if (r.cool > 0) {
           r.cool--;
         } else {
@@ -783,14 +781,20 @@ __device__ __forceinline__ void march_plain_kernel(const F& field, const MarchAr
 
 // --------------------------------------------------------------------------
 // Persistent batched march: many views of uneven size, camera, step size and
-// field in one launch.  Work comes from a device queue: a 64-bit counter over
-// the concatenated ray space of all views (each view's rays ordered in
-// tile_w x tile_h pixel tiles of 32 rays, so consecutive rays are image
-// neighbours).  Each warp owns 32 ray slots; every `quantum` RK4 steps it
-// retires finished rays (storing their pixels) and refills the free slots with
-// one atomicAdd on the counter (persistent "while-while" ray scheduling,
-// Aila & Laine 2009).  Warps exit when the queue is drained and their slots
-// are empty.
+// field in one launch, fed by a device work queue (persistent "while-while"
+// ray scheduling, Aila & Laine 2009).  Each warp is bound to one view at a
+// time, so the view's march parameters, camera and field are uniform across
+// the warp: the field is chosen once per quantum, the camera basis is set up
+// once per binding (in shared memory) and no lane carries per-view state.
+// The queue is one counter per view (BatchView::next) over its rays in
+// tile_w x tile_h tiles of 32 (consecutive rays are image neighbours).  A
+// warp marches `quantum` RK4 steps at a time, retires finished rays (storing
+// their pixels) and refills its free lanes from its view when fewer than
+// refill_below lanes are still marching (or when it is empty); once the view
+// has no rays left the warp finishes its lanes and binds to the next view
+// that has some (views are queued with the largest step budget first, and
+// counter[0] holds the first view that may still have rays).  Warps exit
+// when every view is drained and their lanes are done.
 // --------------------------------------------------------------------------
 template <class F>
 __device__ __forceinline__ void ray_step_rt(RayState& r, const F& field, const DevMarch& m,
@@ -804,125 +808,120 @@ __device__ __forceinline__ void ray_step_rt(RayState& r, const F& field, const D
   }
 }
 
-template <class Fields>
-struct FieldRef {
-  const Fields& f;
-  int i;
-  __device__ __forceinline__ vec3f operator()(const vec3f& pp, const vec3f& p, const vec3f& v0,
-                                              const vec3f& v, float t) const {
-    return f(i, pp, p, v0, v, t);
-  }
-};
-
-__device__ __forceinline__ int find_view(const BatchArgs& a, long long gid) {
-  int lo = 0, hi = a.n_views - 1;  // last view with ray_begin <= gid
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (a.views[mid].ray_begin <= gid) lo = mid;
-    else hi = mid - 1;
-  }
-  return lo;
+__device__ __forceinline__ long long view_rays(const BatchArgs& a, int v) {
+  return (v + 1 < a.n_views ? a.views[v + 1].ray_begin : a.total_rays) - a.views[v].ray_begin;
 }
 
-// MODE: 0 any views (the step variant is chosen per ray at run time);
-// 1 every view has a fixed step budget without Kahan sums; 2 the same with
+// First view at or after counter[0] whose queue is not drained (-1: none);
+// drained views at the front advance counter[0].
+__device__ __forceinline__ int next_open_view(const BatchArgs& a) {
+  volatile unsigned long long* cursor = a.counter;
+  int v = int(*cursor);
+  for (; v < a.n_views; ++v) {
+    const volatile unsigned long long* nx = &a.views[v].next;
+    if ((long long)*nx < view_rays(a, v)) break;
+    atomicMax(a.counter, (unsigned long long)(v + 1));
+  }
+  return v < a.n_views ? v : -1;
+}
+
+// MODE: 0 any views (the step variant is chosen per view at run time); 1
+// every view has a fixed step budget without Kahan sums; 2 the same with
 // Kahan sums.  The specialised modes carry no adaptive-step or unused-sum
-// state, which keeps the kernel's register count (and so its occupancy)
-// close to the plain kernel's.
+// state.
+#ifndef LINON_BATCH_MAX_WARPS
+#define LINON_BATCH_MAX_WARPS 8  // 256-thread CTAs at most (LINON_BATCH_BOUNDS)
+#endif
 template <int MODE = 0, class Fields>
 __device__ __forceinline__ void march_batch_kernel(const Fields& fields, const BatchArgs& a) {
   extern __shared__ float4 linon_smem[];
   __shared__ unsigned long long mbar;
+  // each warp's camera basis of its bound view (raw storage: Basis has
+  // constructors, which a __shared__ variable may not run)
+  __shared__ __align__(16) unsigned char warp_basis[LINON_BATCH_MAX_WARPS * sizeof(Basis)];
   const SceneView sc = cta_scene(a.scene, linon_smem, &mbar, a.err);
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
+  Basis& wb = reinterpret_cast<Basis*>(warp_basis)[threadIdx.x >> 5];
   RayState r;
-  DevMarch m;
-  int vi = 0;  // view of the lane's ray (its output planes are read at the store)
-  size_t pix = 0;
-  int fidx = 0;
+  unsigned pix = 0;  // row * W + x (images hold at most 2^31 - 1 pixels)
   bool active = false;
-  bool drained = false;
+  int view = -1;           // warp-uniform: the bound view
+  bool view_open = false;  // warp-uniform: the bound view may still have rays
   for (;;) {
-    // ---- refill free slots from the queue ----
-    if (!drained) {
-      const unsigned free_mask = __ballot_sync(FULL, !active);
-      if (free_mask) {
-        const int nfree = __popc(free_mask);
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(a.counter, (unsigned long long)nfree);
-        base = __shfl_sync(FULL, base, 0);
-        if (base + nfree >= (unsigned long long)a.total_rays) drained = true;
-        if (!active) {
-          const long long gid = (long long)base + __popc(free_mask & ((1u << lane) - 1));
-          if (gid < a.total_rays) {
-            const int view = find_view(a, gid);
-            const BatchView& V = a.views[view];
-            const long long local = gid - V.ray_begin;
-            const int tile = int(local / (a.tile_w * a.tile_h));
-            const int within = int(local % (a.tile_w * a.tile_h));
-            const int x = (tile % V.tiles_x) * a.tile_w + within % a.tile_w;
-            const int row = (tile / V.tiles_x) * a.tile_h + within / a.tile_w;
-            if (x < V.frame.W && row < V.frame.H) {
-              m = V.m;
-              vi = view;
-              fidx = V.field;
-              pix = size_t(row) * V.frame.W + x;
-              const Basis b = make_basis(V.cam, V.frame.W, V.frame.H, m.focal_length, m.viewport_height);
-              const vec3f dir = primary_dir(b, x, V.frame.H - 1 - row);
-              ray_init(r, b.origin, dir, m.h_initial);
-              active = true;
-              if (m.linear_mode) {
-                HitRec hit = intersect_segment(sc, b.origin, dir, 100.0f, b.origin + 100.0f * dir, a.err);
-                wgsl::vec4f c(0.0f, 0.0f, 0.0f, 0.0f);
-                if (hit.t > 0.0f && hit.t < 100.0f) c = shade_hit(sc, hit, dir);
-                const DevFrame& out = V.frame;
-                if (out.color) {
-                  uchar4 o;
-                  o.x = unorm8(c.x); o.y = unorm8(c.y); o.z = unorm8(c.z); o.w = unorm8(c.w);
-                  out.color[pix] = o;
-                }
-                if (out.hit) out.hit[pix] = hit.t > 0.0f && hit.t < 100.0f ? hit.id : -1;
-                if (out.mapping) out.mapping[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                if (out.steps) out.steps[pix] = 0;
-                active = false;
+    unsigned act = __ballot_sync(FULL, active);
+    // ---- bind the next view with rays when the warp is empty ----
+    if (act == 0u && !view_open) {
+      view = 0;
+      if (lane == 0) view = next_open_view(a);
+      view = __shfl_sync(FULL, view, 0);
+      if (view < 0) break;
+      view_open = true;
+      __syncwarp();  // every lane is done with the previous view's basis
+      if (lane == 0) {
+        const BatchView& V = a.views[view];
+        wb = make_basis(V.cam, V.frame.W, V.frame.H, V.m.focal_length, V.m.viewport_height);
+      }
+      __syncwarp();
+    }
+    const BatchView& V = a.views[view];
+    const DevMarch m = V.m;
+    // ---- refill free lanes from the bound view ----
+    if (view_open && (act == 0u || __popc(act) < a.refill_below)) {
+      const int nfree = 32 - __popc(act);
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(&a.views[view].next, (unsigned long long)nfree);
+      base = __shfl_sync(FULL, base, 0);
+      const long long n_rays = view_rays(a, view);
+      if ((long long)(base + nfree) >= n_rays) view_open = false;
+      if (!active) {
+        const long long local = (long long)base + __popc(~act & ((1u << lane) - 1));
+        if (local < n_rays) {
+          const int tile = int(local / (a.tile_w * a.tile_h));
+          const int within = int(local % (a.tile_w * a.tile_h));
+          const int x = (tile % V.tiles_x) * a.tile_w + within % a.tile_w;
+          const int row = (tile / V.tiles_x) * a.tile_h + within / a.tile_w;
+          if (x < V.frame.W && row < V.frame.H) {
+            pix = unsigned(row) * unsigned(V.frame.W) + unsigned(x);
+            ray_init(r, wb.origin, primary_dir(wb, x, V.frame.H - 1 - row), m.h_initial);
+            active = true;
+            if (m.linear_mode) {
+              HitRec hit = intersect_segment<true>(sc, wb.origin, r.dir, 100.0f, wb.origin + 100.0f * r.dir, a.err);
+              wgsl::vec4f c(0.0f, 0.0f, 0.0f, 0.0f);
+              if (hit.t > 0.0f && hit.t < 100.0f) c = shade_hit(sc, hit, r.dir);
+              const DevFrame& out = V.frame;
+              if (out.color) {
+                uchar4 o;
+                o.x = unorm8(c.x); o.y = unorm8(c.y); o.z = unorm8(c.z); o.w = unorm8(c.w);
+                out.color[pix] = o;
               }
+              if (out.hit) out.hit[pix] = hit.t > 0.0f && hit.t < 100.0f ? hit.id : -1;
+              if (out.mapping) out.mapping[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+              if (out.steps) out.steps[pix] = 0;
+              active = false;
             }
           }
         }
       }
+      act = __ballot_sync(FULL, active);
     }
-    if (!__any_sync(FULL, active)) {
-      if (drained) break;
-      continue;
-    }
-    // ---- march a quantum (one warp vote per step keeps the lanes converged;
-    //      the warp leaves early to refill once fewer than refill_below lanes
-    //      are still marching and the queue has work) ----
-    auto quantum = [&](const auto& field) {
+    if (act == 0u) continue;  // nothing to march: refill again or bind the next view
+    // ---- march a quantum with the view's field (uniform across the warp);
+    //      a warp whose view still has rays leaves early to refill once
+    //      fewer than refill_below lanes are marching ----
+    fields.visit(V.field, [&](const auto& field) {
       for (int q = 0; q < a.quantum; ++q) {
         const bool go = active && ray_active(r, m);
         const unsigned g = __ballot_sync(FULL, go);
-        if (g == 0u || (!drained && __popc(g) < a.refill_below)) break;
+        if (g == 0u || (view_open && __popc(g) < a.refill_below)) break;
         if (go) {
           if (MODE == 0) ray_step_rt(r, field, m, sc, a.err);
           else ray_step<false, MODE == 2, false, true>(r, field, m, sc, a.err);
         }
       }
-    };
-    // A warp whose marching lanes share one field (the rule: a warp refills
-    // 32 consecutive rays of the queue, which lie in one view unless they
-    // straddle a view boundary) runs the quantum with that field's loop;
-    // a mixed warp chooses the field per lane in every evaluation (64
-    // uneven views, quantum 1024: 18.7 -> 13.5 ms).
-    const unsigned act = __ballot_sync(FULL, active);
-    const int f0 = __shfl_sync(FULL, fidx, __ffs(act) - 1);
-    if (MODE != 0 && __all_sync(FULL, !active || fidx == f0))
-      fields.visit(f0, quantum);
-    else
-      quantum(FieldRef<Fields>{fields, fidx});
+    });
     if (active && !ray_active(r, m)) {
-      ray_store(r, a.views[vi].frame, pix);
+      ray_store(r, V.frame, pix);
       active = false;
     }
   }

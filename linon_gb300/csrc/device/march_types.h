@@ -83,14 +83,17 @@ struct BatchView {
   DevFrame frame;
   int block_begin;     // first CTA of this view in a one-CTA-per-tile launch
   int blocks_x;        // 8 x 16-pixel CTA tiles per image row
+  // persistent queue: the view's next ray to hand out (the host uploads the
+  // table with 0 before every launch; warps take rays with atomicAdd)
+  unsigned long long next;
 };
 
 struct BatchArgs {
-  const BatchView* views;
+  BatchView* views;
   int n_views;
   int quantum;             // RK4 steps between retire/refill
   long long total_rays;
-  unsigned long long* counter;  // queue head (zeroed before the launch)
+  unsigned long long* counter;  // persistent queue: [0] first view that may have rays (zeroed before the launch)
   DevScene scene;
   int tile_w, tile_h;      // tile_w * tile_h == 32
   int refill_below;        // leave the quantum early below this many marching lanes

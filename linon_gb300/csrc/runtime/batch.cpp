@@ -277,7 +277,7 @@ const char* batch_kernel_name(const linon_view* views, int n_views, int schedule
 }
 
 int batch_launch(linon_ctx* ctx, const std::shared_ptr<JitModule>& mod, const linon_batch_tuning& t,
-                 const BatchView* views_dev, int n_views, long long total_rays, int n_blocks,
+                 BatchView* views_dev, int n_views, long long total_rays, int n_blocks,
                  unsigned long long* counter, cudaStream_t stream, const char* kernel) {
   BatchArgs a;
   std::memset(&a, 0, sizeof a);
@@ -355,7 +355,7 @@ int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields, int32_t
                                cudaMemcpyHostToDevice, ctx->stream));
     BatchArgs a;
     std::memset(&a, 0, sizeof a);
-    a.views = static_cast<const BatchView*>(bs.views.p);
+    a.views = static_cast<BatchView*>(bs.views.p);
     a.n_views = n_views;
     a.quantum = t.quantum;
     a.total_rays = begin;

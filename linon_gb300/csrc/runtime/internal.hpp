@@ -104,7 +104,7 @@ int batch_module(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fie
 // otherwise the generic linon_batch.
 const char* batch_kernel_name(const linon_view* views, int n_views, int schedule);
 int batch_launch(linon_ctx* ctx, const std::shared_ptr<JitModule>& mod, const linon_batch_tuning& t,
-                 const BatchView* views_dev, int n_views, long long total_rays, int n_blocks,
+                 BatchView* views_dev, int n_views, long long total_rays, int n_blocks,
                  unsigned long long* counter, cudaStream_t stream, const char* kernel);
 
 }  // namespace linon

@@ -62,6 +62,34 @@ __device__ __forceinline__ T lyapunov(const float4* mapping, int W, int x, int y
   return sqrt(fmax(e0, e1));
 }
 
+// The overlay's exponent with FP64 where differencing cancels: the central
+// differences of the endpoints (FP32 values, so each difference is exact in
+// FP64) and the 2x2 matrix M = G^T G built from them, including its
+// determinant m00 m11 - m01^2, which cancels when G is close to rank one.
+// The eigenvalue of mat2eigenvalues (overlay.wgsl:4-40) that the exponent
+// takes, the larger root of x^2 - tr x + det, is well conditioned in the
+// rounded trace and determinant, so it and the square roots run in FP32.
+// G = D / 2 is folded in: tr(M) = tr(D^T D) / 4, det(M) = det(D^T D) / 16.
+__device__ __forceinline__ float lyapunov_fp64_diff(const float4* mapping, int W, int x, int y, int delta) {
+  const float4 xn = mapping[size_t(y) * W + (x + delta)], xp = mapping[size_t(y) * W + (x - delta)];
+  const float4 yn = mapping[size_t(y + delta) * W + x], yp = mapping[size_t(y - delta) * W + x];
+  const double d00 = double(xn.x) - double(xp.x), d01 = double(xn.y) - double(xp.y),
+               d02 = double(xn.z) - double(xp.z);
+  const double d10 = double(yn.x) - double(yp.x), d11 = double(yn.y) - double(yp.y),
+               d12 = double(yn.z) - double(yp.z);
+  const double m00 = fma(d02, d02, fma(d01, d01, d00 * d00));
+  const double m01 = fma(d02, d12, fma(d01, d11, d00 * d10));
+  const double m11 = fma(d12, d12, fma(d11, d11, d10 * d10));
+  const float det = float(fma(m00, m11, -(m01 * m01)) * 0.0625);
+  const float tr = float((m00 + m11) * 0.25);
+  const float a1 = -tr;
+  const float discrim = a1 * a1 - 4.0f * det;
+  float e;
+  if (discrim >= 0.0f) e = (-a1 + sqrtf(discrim)) * 0.5f;  // the larger root
+  else e = fmaxf(-a1 * 0.5f, sqrtf(-discrim) * 0.5f);
+  return sqrtf(e);
+}
+
 template <bool FP64>
 __global__ void overlay_kernel(OverlayArgs a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -75,8 +103,8 @@ __global__ void overlay_kernel(OverlayArgs a) {
       a.mode == 1) {
     float scaled;
     if (FP64) {
-      double e = lyapunov<double>(a.mapping, a.W, x, y, a.delta);
-      scaled = float(exp(double(a.scaling) * e - 5.0));
+      const float e = lyapunov_fp64_diff(a.mapping, a.W, x, y, a.delta);
+      scaled = expf(a.scaling * e - 5.0f);
     } else {
       float e = lyapunov<float>(a.mapping, a.W, x, y, a.delta);
       scaled = expf(a.scaling * e - 5.0f);
@@ -133,24 +161,32 @@ __global__ void ftle_kernel(FtleArgs a) {
   float dc[3];
   primary_dir(b, x, a.H - 1 - y, dc);
   const float4 ec = a.mapping[ci];
+  const double cx = double(ec.x), cy = double(ec.y), cz = double(ec.z);
   const int dx[4] = {1, -1, 0, 0}, dy[4] = {0, 0, 1, -1};
-  double best = -1.0;
+  // The largest ratio |e(nb) - e(c)|^2 / |d0(nb) - d0(c)|^2: endpoint
+  // differences and their squared lengths in FP64 (exact differences of
+  // FP32 values; neighbouring endpoints cancel); the initial separations of
+  // the FP32 primary directions in FP32 (neighbouring directions are within
+  // a factor of two, so their difference is exact, and its squared length is
+  // well conditioned).  Candidates are compared by cross-multiplication, and
+  // the ratio and its logarithm are taken once, in FP64.
+  double best_de = -1.0, best_dd = 1.0;
   for (int k = 0; k < 4; ++k) {
     const int nx = x + dx[k], ny = y + dy[k];
     if (nx < 0 || ny < 0 || nx >= a.W || ny >= a.H) continue;
     const float4 en = a.mapping[size_t(ny) * a.W + nx];
     float dn[3];
     primary_dir(b, nx, a.H - 1 - ny, dn);
-    const double e0 = double(en.x) - double(ec.x), e1 = double(en.y) - double(ec.y),
-                 e2 = double(en.z) - double(ec.z);
-    const double q0 = double(dn[0]) - double(dc[0]), q1 = double(dn[1]) - double(dc[1]),
-                 q2 = double(dn[2]) - double(dc[2]);
-    const double de = (e0 * e0 + e1 * e1) + e2 * e2;
-    const double dd = (q0 * q0 + q1 * q1) + q2 * q2;
-    const double r = sqrt(de) / sqrt(dd);
-    if (r > best) best = r;
+    const double e0 = double(en.x) - cx, e1 = double(en.y) - cy, e2 = double(en.z) - cz;
+    const double de = fma(e2, e2, fma(e1, e1, e0 * e0));
+    const float q0 = dn[0] - dc[0], q1 = dn[1] - dc[1], q2 = dn[2] - dc[2];
+    const double dd = double((q0 * q0 + q1 * q1) + q2 * q2);
+    if (de * best_dd > best_de * dd) {
+      best_de = de;
+      best_dd = dd;
+    }
   }
-  a.out[ci] = best > 0.0 ? float(log(best) / a.T) : -__int_as_float(0x7f800000);
+  a.out[ci] = best_de > 0.0 ? float(0.5 * log(best_de / best_dd) / a.T) : -__int_as_float(0x7f800000);
 }
 
 // Outline selection.  Each of the shader's 8 scans picks either the last
