@@ -134,6 +134,7 @@ PROTOTYPES = {
     "linon_field_compile": (C.c_int, [vp, cp, cp, C.c_int, P(vp), C.c_char_p, sz]),
     "linon_field_release": (C.c_int, [vp, vp]),
     "linon_field_flops": (C.c_int, [vp, P(i32), P(i32)]),
+    "linon_field_pair_state": (C.c_int, [vp]),
     "linon_field_cuda_source": (cp, [vp]),
     "linon_field_validate": (C.c_int, [cp, cp, C.c_int, C.c_char_p, sz]),
     "linon_wgsl_translate": (C.c_int, [cp, cp, C.c_char_p, sz, C.c_char_p, sz]),

@@ -502,8 +502,44 @@ __device__ __forceinline__ bool ray_active(const RayState& r, const DevMarch& m)
 // combination): adaptive refinement, Kahan sums, fixed step budget (with it
 // the compiler drops the time accumulator when the field ignores t), and
 // field_weight == 1 in fast modules (the blend is then dir = v, identical
-// for finite directions).
-enum { V_ADAPTIVE = 1, V_KAHAN = 2, V_STEPS = 4, V_W1 = 8 };
+// for finite directions).  V_PAIRS: two rays per thread (march_pair_kernel).
+enum { V_ADAPTIVE = 1, V_KAHAN = 2, V_STEPS = 4, V_W1 = 8, V_PAIRS = 16 };
+
+// The segment [p, p + step_dir) of a ray that has not hit yet and whose end
+// left its safe ball: the intersection test (ray_color, main_view.wgsl:
+// 177-220, through the candidate lists or the BVH), the shading of a hit, and
+// a new safe ball around the segment's end (or, close to geometry, plain
+// tests for the next 8 segments).
+template <bool PAIR>
+__device__ __forceinline__ void segment_test(const SceneView& sc, const vec3f& p, const vec3f& step_dir,
+                                             const vec3f& seg_end, bool& has_color, wgsl::vec4f& color,
+                                             int& face, vec3f& q0, float& safe2, int& cool, int* err) {
+  const float len = wgsl::length(step_dir);
+#if defined(LINON_PRECISE)
+  const vec3f dirn = step_dir / len;
+#else
+  const vec3f dirn = wgsl::normalize(step_dir);
+#endif
+  HitRec hit = intersect_segment_cells<PAIR>(sc, p, dirn, len, seg_end, err);
+  if (hit.t > 0.0f && hit.t < len) {
+    color = shade_hit(sc, hit, dirn);
+    has_color = color.w > 0.0f;
+    if (has_color) face = hit.id;
+  }
+  safe2 = -1.0f;
+  if (!has_color && sc.n_nodes > 0) {
+    if (cool > 0) {
+      cool--;
+    } else {
+      // a new ball around the segment's end, where the next one starts
+      const float b = safe_radius(sc, seg_end);
+      q0 = seg_end;
+      safe2 = b * b;
+      // close to geometry the ball buys little: test plainly for a while
+      if (b < 4.0f * len) cool = 8;
+    }
+  }
+}
 
 // One attempted RK4 step (main_view.wgsl:245-270).  Returns false when the
 // step was rejected by the adaptive rule (h refined, nothing advanced).
@@ -549,33 +585,8 @@ __device__ __forceinline__ bool ray_step(RayState& r, const F& field, const DevM
   if (!r.has_color) {
     const vec3f seg_end = wgsl::vadd(r.p, step_dir);
     const vec3f dq = wgsl::vsub(seg_end, r.q0);
-    if (!(wgsl::dot(dq, dq) <= r.safe2)) {
-      const float len = wgsl::length(step_dir);
-#if defined(LINON_PRECISE)
-      const vec3f dirn = step_dir / len;
-#else
-      const vec3f dirn = wgsl::normalize(step_dir);
-#endif
-      HitRec hit = intersect_segment_cells<PAIR>(sc, r.p, dirn, len, seg_end, err);
-      if (hit.t > 0.0f && hit.t < len) {
-        r.color = shade_hit(sc, hit, dirn);
-        r.has_color = r.color.w > 0.0f;
-        if (r.has_color) r.face = hit.id;
-      }
-      r.safe2 = -1.0f;
-      if (!r.has_color && sc.n_nodes > 0) {
-        if (r.cool > 0) {
-          r.cool--;
-        } else {
-          // a new ball around the segment's end, where the next one starts
-          const float b = safe_radius(sc, seg_end);
-          r.q0 = seg_end;
-          r.safe2 = b * b;
-          // close to geometry the ball buys little: test plainly for a while
-          if (b < 4.0f * len) r.cool = 8;
-        }
-      }
-    }
+    if (!(wgsl::dot(dq, dq) <= r.safe2))
+      segment_test<PAIR>(sc, r.p, step_dir, seg_end, r.has_color, r.color, r.face, r.q0, r.safe2, r.cool, err);
   }
   if (KAHAN) {
     kahan_add3(r.p, r.cp, step_dir);
@@ -778,6 +789,153 @@ __device__ __forceinline__ void march_plain_kernel(const F& field, const MarchAr
   }
   if (in_image) ray_store(r, a.frame, idx);
 }
+
+#if defined(LINON_PAIRS) && defined(LINON_F32X2)
+// --------------------------------------------------------------------------
+// Two rays per thread: the fixed-step march (no adaptive retries, no stop at
+// the first hit) of two horizontally adjacent pixels, their arithmetic
+// issued as packed FP32 pairs (wgsl::f2) with the field function emitted in
+// pair form.  Per pair of rays the thread issues the field evaluations, the
+// RK4 average, the step, the safe-ball test and the Kahan sums once instead
+// of twice, and the loop and reconvergence bookkeeping once; the march is
+// issue-bound in one-ray form (twist, linear) or close to it (lens).  Each
+// operation rounds like the one-ray fast kernel's, whose multiply-adds the
+// compiler contracts where these are written as packed FMAs.  The segment
+// test of a ray that left its safe ball runs on that ray's values alone
+// (segment_test, as in ray_step); a hit's colour and face are stored at
+// once, so no shading state is carried through the loop.  The CTA covers
+// tile_w x tile_h pixels with tile_w / 2 x tile_h threads.
+// --------------------------------------------------------------------------
+using wgsl::f2;
+using wgsl::vec3p;
+
+__device__ __forceinline__ vec3p pack_pair(const vec3f& a, const vec3f& b) {
+  return vec3p(f2(a.x, b.x), f2(a.y, b.y), f2(a.z, b.z));
+}
+__device__ __forceinline__ vec3f pair_lane(const vec3p& v, int k) {
+  return k ? vec3f(v.x.v.y, v.y.v.y, v.z.v.y) : vec3f(v.x.v.x, v.y.v.x, v.z.v.x);
+}
+__device__ __forceinline__ void kahan_add_pair(f2& sum, f2& c, f2 x) {
+  const f2 y = x - c;
+  const f2 t = sum + y;
+  c = (t - sum) - y;
+  sum = t;
+}
+
+template <int V, class F>
+__device__ __forceinline__ void march_pair_kernel(const F& field, const MarchArgs& a) {
+  constexpr bool KAHAN = (V & V_KAHAN) != 0;
+  constexpr bool W1 = (V & V_W1) != 0;
+  extern __shared__ float4 linon_smem[];
+  __shared__ unsigned long long mbar;
+  const SceneView sc = cta_scene(a.scene, linon_smem, &mbar, a.err);
+  const int W = a.frame.W, H = a.frame.H;
+  const int pairs_w = a.tile_w / 2;
+  const int lx = threadIdx.x % pairs_w, ly = threadIdx.x / pairs_w;
+  const int x0 = blockIdx.x * a.tile_w + 2 * lx;
+  const int row = a.row0 + blockIdx.y * a.tile_h + ly;
+  // lanes outside the image march pixel (0, 0)'s ray and store nothing
+  const bool in0 = x0 < W && row < a.row1, in1 = x0 + 1 < W && row < a.row1;
+  const int gy = H - 1 - row;
+  const Basis b = make_basis(a.cam, W, H, a.m.focal_length, a.m.viewport_height);
+  const vec3f d0 = primary_dir(b, in0 ? x0 : 0, in0 ? gy : 0);
+  const vec3f d1 = primary_dir(b, in1 ? x0 + 1 : 0, in1 ? gy : 0);
+  const size_t idx0 = in0 ? size_t(row) * W + x0 : 0, idx1 = idx0 + 1;
+  vec3p p = pack_pair(b.origin, b.origin), dir = pack_pair(d0, d1);
+  const vec3p v0 = dir;
+  vec3p cp(f2(0.0f), f2(0.0f), f2(0.0f));
+  f2 t(0.0f), ct(0.0f);
+  const f2 h(a.m.h_initial), hh(0.5f * a.m.h_initial);
+  vec3p q0 = p;
+  f2 safe2(-1.0f);
+  bool has0 = false, has1 = false;
+  int cool0 = 0, cool1 = 0;
+  for (int s = 0; s < a.m.max_steps; ++s) {
+    const vec3p k1 = field(p, p, v0, dir, t);
+    const vec3p k2 = field(p, vec3p(p + hh * k1), v0, k1, t + hh);
+    const vec3p k3 = field(p, vec3p(p + hh * k2), v0, k2, t + hh);
+    const vec3p k4 = field(p, vec3p(p + h * k3), v0, k3, t + h);
+    // (((k1 + 2 k2) + 2 k3) + k4) / 6, as rk4_combine
+    const vec3p sum = (vec3p(k1 + f2(2.0f) * k2) + f2(2.0f) * k3) + k4;
+    const vec3p v = sum * f2(1.0f / 6.0f);
+    if (W1) {
+      dir = v;
+    } else {
+      const f2 w(a.m.field_weight);
+      dir = vec3p((f2(1.0f) - w) * dir) + v * w;
+    }
+    const vec3p step_dir = dir * h;
+    if (!(has0 && has1)) {
+      const vec3p seg_end = p + step_dir;
+      const vec3p dq = seg_end - q0;
+      const f2 d2 = wgsl::dot(dq, dq);
+      const bool need0 = !has0 && !(d2.v.x <= safe2.v.x);
+      const bool need1 = !has1 && !(d2.v.y <= safe2.v.y);
+      if (need0 || need1) {
+#pragma unroll 1
+        for (int k = 0; k < 2; ++k) {
+          if (!(k ? need1 : need0)) continue;
+          bool has = false;
+          wgsl::vec4f color(0.0f, 0.0f, 0.0f, 0.0f);
+          int face = -1;
+          vec3f q = pair_lane(q0, k);
+          float sf = k ? safe2.v.y : safe2.v.x;
+          int cool = k ? cool1 : cool0;
+          segment_test<false>(sc, pair_lane(p, k), pair_lane(step_dir, k), pair_lane(seg_end, k), has, color, face, q,
+                              sf, cool, a.err);
+          if (has && (k ? in1 : in0)) {  // the first hit decides the pixel's colour and face
+            const size_t idx = k ? idx1 : idx0;
+            if (a.frame.color) {
+              uchar4 c;
+              c.x = unorm8(color.x);
+              c.y = unorm8(color.y);
+              c.z = unorm8(color.z);
+              c.w = 255;
+              a.frame.color[idx] = c;
+            }
+            if (a.frame.hit) a.frame.hit[idx] = face;
+          }
+          if (k) {
+            has1 = has;
+            cool1 = cool;
+            q0.x.v.y = q.x; q0.y.v.y = q.y; q0.z.v.y = q.z;
+            safe2.v.y = sf;
+          } else {
+            has0 = has;
+            cool0 = cool;
+            q0.x.v.x = q.x; q0.y.v.x = q.y; q0.z.v.x = q.z;
+            safe2.v.x = sf;
+          }
+        }
+      }
+    }
+    if (KAHAN) {
+      kahan_add_pair(p.x, cp.x, step_dir.x);
+      kahan_add_pair(p.y, cp.y, step_dir.y);
+      kahan_add_pair(p.z, cp.z, step_dir.z);
+      kahan_add_pair(t, ct, h);
+    } else {
+      p = p + step_dir;
+      t = t + h;
+    }
+    __syncwarp();
+  }
+  // final stores of main_view.wgsl:373-374 (a hit's colour was stored above)
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    if (!(k ? in1 : in0)) continue;
+    const size_t idx = k ? idx1 : idx0;
+    const bool has = k ? has1 : has0;
+    if (!has) {
+      if (a.frame.color) a.frame.color[idx] = make_uchar4(0, 0, 0, 255);
+      if (a.frame.hit) a.frame.hit[idx] = -1;
+    }
+    const vec3f e = pair_lane(p, k);
+    if (a.frame.mapping) a.frame.mapping[idx] = make_float4(e.x, e.y, e.z, 1.0f);
+    if (a.frame.steps) a.frame.steps[idx] = a.m.max_steps;
+  }
+}
+#endif  // LINON_PAIRS
 
 // --------------------------------------------------------------------------
 // Persistent batched march: many views of uneven size, camera, step size and

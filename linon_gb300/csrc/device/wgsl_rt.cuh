@@ -1144,4 +1144,164 @@ WG_HD float point_plane_distance(const vec3f& p, const vec3f& n, const vec3f& p0
 }
 WG_HD float sigmoid(float x) { return 1.0f / (1.0f + expf(-x)); }  // main_view.wgsl:144-146
 
+// ---------------------------------------------------------------------------
+// Two rays per thread (fast modules that define LINON_PAIRS, sm_100 and
+// later).  An f2 is one f32 value of two rays (x: the first, y: the
+// second); the front end's pair emission writes a field function over f2,
+// and every operation runs lane-wise as one packed FP32 pair instruction
+// (f32x2, each lane rounded like the scalar operation) or as two scalar
+// ones where there is no packed form (division, square roots, the special
+// functions).  a * b is kept unevaluated until it meets + or -, which then
+// issue one packed FMA, as the compiler contracts the scalar code.  There is
+// deliberately no comparison, no conversion to an integer and no conversion
+// back to float: a field that needs one fails to compile in pair form and
+// runs one ray per thread.
+// ---------------------------------------------------------------------------
+#if defined(LINON_PAIRS) && defined(LINON_F32X2)
+struct f2 {
+  float2 v;
+  WG_HD f2() : v(make_float2(0.0f, 0.0f)) {}
+  WG_HD f2(float s) : v(make_float2(s, s)) {}
+  WG_HD f2(float a, float b) : v(make_float2(a, b)) {}
+  WG_HD explicit f2(float2 p) : v(p) {}
+};
+WG_HD f2 neg(f2 a) { return f2(make_float2(-a.v.x, -a.v.y)); }
+WG_HD f2 fma2(f2 a, f2 b, f2 c) { return f2(__ffma2_rn(a.v, b.v, c.v)); }
+WG_HD f2 mul2(f2 a, f2 b) { return f2(__fmul2_rn(a.v, b.v)); }
+struct f2m {  // a * b, not yet rounded
+  f2 a, b;
+  WG_HD operator f2() const { return mul2(a, b); }
+};
+WG_HD f2m operator*(f2 a, f2 b) { return f2m{a, b}; }
+WG_HD f2 operator+(f2 a, f2 b) { return f2(__fadd2_rn(a.v, b.v)); }
+WG_HD f2 operator-(f2 a, f2 b) { return f2(__fadd2_rn(a.v, neg(b).v)); }
+WG_HD f2 operator+(f2m m, f2 c) { return fma2(m.a, m.b, c); }
+WG_HD f2 operator+(f2 c, f2m m) { return fma2(m.a, m.b, c); }
+WG_HD f2 operator-(f2m m, f2 c) { return fma2(m.a, m.b, neg(c)); }
+WG_HD f2 operator-(f2 c, f2m m) { return fma2(neg(m.a), m.b, c); }
+WG_HD f2 operator+(f2m m, f2m n) { return fma2(m.a, m.b, f2(n)); }
+WG_HD f2 operator-(f2m m, f2m n) { return fma2(m.a, m.b, neg(f2(n))); }
+WG_HD f2 operator-(f2 a) { return neg(a); }
+WG_HD f2 operator-(f2m m) { return mul2(neg(m.a), m.b); }
+WG_HD f2 operator/(f2 a, f2 b) { return f2(a.v.x / b.v.x, a.v.y / b.v.y); }
+WG_HD f2& operator+=(f2& a, f2 b) { a = a + b; return a; }
+WG_HD f2& operator-=(f2& a, f2 b) { a = a - b; return a; }
+WG_HD f2& operator*=(f2& a, f2 b) { a = mul2(a, b); return a; }
+WG_HD f2& operator/=(f2& a, f2 b) { a = a / b; return a; }
+#define WG_F2_LANES(NAME, EXPR)                                                    \
+  WG_HD f2 NAME(f2 a) {                                                            \
+    const float x0 = a.v.x, x1 = a.v.y;                                            \
+    float r0, r1;                                                                  \
+    { const float x = x0; r0 = (EXPR); }                                           \
+    { const float x = x1; r1 = (EXPR); }                                           \
+    return f2(r0, r1);                                                             \
+  }
+WG_F2_LANES(sqrt, sqrtf(x))
+WG_F2_LANES(inverseSqrt, rsqrt_ftz(x))
+WG_F2_LANES(rsqrt_ftz2, rsqrt_ftz(x))
+WG_F2_LANES(abs, fabsf(x))
+WG_F2_LANES(exp, expf(x))
+WG_F2_LANES(sin, sin_(x))
+WG_F2_LANES(cos, cos_(x))
+WG_F2_LANES(floor, floorf(x))
+WG_F2_LANES(length, fabsf(x))
+#undef WG_F2_LANES
+WG_HD f2 min(f2 a, f2 b) { return f2(fminf(a.v.x, b.v.x), fminf(a.v.y, b.v.y)); }
+WG_HD f2 max(f2 a, f2 b) { return f2(fmaxf(a.v.x, b.v.x), fmaxf(a.v.y, b.v.y)); }
+WG_HD f2 clamp(f2 e, f2 lo, f2 hi) { return min(max(e, lo), hi); }
+WG_HD f2 sigmoid(f2 x) { return f2(1.0f) / (f2(1.0f) + exp(neg(x))); }
+WG_HD void sincos2(f2 x, f2* s, f2* c) {
+  float s0, c0, s1, c1;
+  sincos_(x.v.x, &s0, &c0);
+  sincos_(x.v.y, &s1, &c1);
+  *s = f2(s0, s1);
+  *c = f2(c0, c1);
+}
+
+typedef vec<f2, 3> vec3p;
+// s * v (or v * s), not yet rounded: + or - with a vector issues packed FMAs
+struct vs2 {
+  vec3p v;
+  f2 s;
+  WG_HD operator vec3p() const { return vec3p(mul2(v.x, s), mul2(v.y, s), mul2(v.z, s)); }
+};
+WG_HD vs2 operator*(const vec3p& v, f2 s) { return vs2{v, s}; }
+WG_HD vs2 operator*(f2 s, const vec3p& v) { return vs2{v, s}; }
+WG_HD vs2 operator*(const vec3p& v, float s) { return vs2{v, f2(s)}; }
+WG_HD vs2 operator*(float s, const vec3p& v) { return vs2{v, f2(s)}; }
+WG_HD vs2 operator*(const vec3p& v, f2m s) { return vs2{v, f2(s)}; }
+WG_HD vs2 operator*(f2m s, const vec3p& v) { return vs2{v, f2(s)}; }
+WG_HD vec3p operator+(const vec3p& a, const vs2& m) {
+  return vec3p(fma2(m.v.x, m.s, a.x), fma2(m.v.y, m.s, a.y), fma2(m.v.z, m.s, a.z));
+}
+WG_HD vec3p operator+(const vs2& m, const vec3p& a) { return a + m; }
+WG_HD vec3p operator-(const vec3p& a, const vs2& m) {
+  const f2 ns = neg(m.s);
+  return vec3p(fma2(m.v.x, ns, a.x), fma2(m.v.y, ns, a.y), fma2(m.v.z, ns, a.z));
+}
+WG_HD vec3p operator-(const vs2& m, const vec3p& a) {
+  return vec3p(fma2(m.v.x, m.s, neg(a.x)), fma2(m.v.y, m.s, neg(a.y)), fma2(m.v.z, m.s, neg(a.z)));
+}
+WG_HD vec3p operator+(const vs2& m, const vs2& n) { return vec3p(m) + n; }
+WG_HD vec3p operator-(const vs2& m, const vs2& n) { return vec3p(m) - n; }
+WG_HD vec3p operator-(const vs2& m) { return vec3p(m.v.x * neg(m.s), m.v.y * neg(m.s), m.v.z * neg(m.s)); }
+WG_HD vec3p operator/(const vec3p& v, f2 s) { return v * (f2(1.0f) / s); }
+WG_HD vec3p operator/(const vec3p& v, float s) { return v * f2(1.0f / s); }
+WG_HD vec3p operator+(const vec3p& v, float s) { return v + vec3p(f2(s)); }
+WG_HD vec3p operator-(const vec3p& v, float s) { return v - vec3p(f2(s)); }
+
+WG_HD f2 dot(const vec3p& a, const vec3p& b) { return fma2(a.z, b.z, fma2(a.y, b.y, mul2(a.x, b.x))); }
+WG_HD f2 dot_add(const vec3p& a, const vec3p& b, f2 s) {
+  return fma2(a.z, b.z, fma2(a.y, b.y, fma2(a.x, b.x, s)));
+}
+WG_HD f2 length(const vec3p& v) { return sqrt(dot(v, v)); }
+WG_HD vec3p normalize(const vec3p& v) { return vec3p(v * rsqrt_ftz2(dot(v, v))); }
+WG_HD vec3p cross(const vec3p& a, const vec3p& b) {
+  return vec3p(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+WG_HD f2 pow_k(f2 x, float k) {
+  if (k == 1.0f) return x;
+  if (k == 2.0f) return mul2(x, x);
+  if (k == 3.0f) return mul2(mul2(x, x), x);
+  if (k == 4.0f) { const f2 y = mul2(x, x); return mul2(y, y); }
+  if (k == 0.5f) return sqrt(x);
+  if (k == 1.5f) return mul2(x, sqrt(x));
+  if (k == -0.5f) return rsqrt_ftz2(x);
+  if (k == -1.0f) return f2(1.0f) / x;
+  if (k == -1.5f) { const f2 r = rsqrt_ftz2(x); return mul2(mul2(r, r), r); }
+  if (k == -2.0f) { const f2 r = f2(1.0f) / x; return mul2(r, r); }
+  if (k == -3.0f) { const f2 r = f2(1.0f) / x; return mul2(mul2(r, r), r); }
+  return f2(powf(x.v.x, k), powf(x.v.y, k));
+}
+WG_HD f2 scaled_pow_neg_k(f2 s, f2 x, float k) {
+  if (k == 1.5f) {
+    const f2 r = rsqrt_ftz2(x);
+    return mul2(mul2(s, r), mul2(r, r));
+  }
+  return mul2(s, pow_k(x, -k));
+}
+WG_HD vs2 div_pow_k_sv(f2 s, const vec3p& v, f2 x, float k) { return vs2{v, scaled_pow_neg_k(s, x, k)}; }
+WG_HD vs2 div_pow_k_vs(const vec3p& v, f2 s, f2 x, float k) { return vs2{v, scaled_pow_neg_k(s, x, k)}; }
+WG_HD vs2 div_pow_k(const vec3p& a, f2 x, float k) { return vs2{a, pow_k(x, -k)}; }
+WG_HD f2 div_pow_k(f2 a, f2 x, float k) { return mul2(a, pow_k(x, -k)); }
+// the linon helpers (main_view.wgsl:78-108), lane-wise, structural zeros
+// left out as in the one-ray fast modules
+WG_HD vec3p rotateX(const vec3p& v, f2 phi) {
+  f2 s, c;
+  sincos2(phi, &s, &c);
+  return vec3p(v.x, c * v.y - s * v.z, s * v.y + c * v.z);
+}
+WG_HD vec3p rotateY(const vec3p& v, f2 phi) {
+  f2 s, c;
+  sincos2(phi, &s, &c);
+  return vec3p(c * v.x + s * v.z, v.y, c * v.z - s * v.x);
+}
+WG_HD vec3p rotateZ(const vec3p& v, f2 phi) {
+  f2 s, c;
+  sincos2(phi, &s, &c);
+  return vec3p(c * v.x - s * v.y, s * v.x + c * v.y, f2(0.0f));
+}
+WG_HD vec3p translate(const vec3p& v, f2 dx, f2 dy, f2 dz) { return vec3p(v.x + dx, v.y + dy, v.z + dz); }
+#endif  // LINON_PAIRS
+
 }  // namespace wgsl

@@ -5,6 +5,7 @@
 // every failure becomes a status code plus linon_last_error().
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <sstream>
 #include <string>
@@ -207,6 +208,24 @@ extern "C" __global__ void __launch_bounds__(256) linon_field_eval(const float* 
   return s.str();
 }
 
+// Module source of a two-ray march variant (V_PAIRS): the field in pair
+// form and march_pair_kernel.
+std::string module_source_pair(const std::string& field_pair_cuda, int v) {
+  std::ostringstream s;
+  s << "#define LINON_PAIRS 1\n#include \"march.cuh\"\n" << field_pair_cuda << R"LINON(
+struct LinonFieldPair {
+  mutable linon_user::Private pv;  // two rays' var<private> state, lane-wise
+  __device__ __forceinline__ wgsl::vec3p operator()(const wgsl::vec3p& pp, const wgsl::vec3p& p,
+      const wgsl::vec3p& v0, const wgsl::vec3p& v, wgsl::f2 t) const {
+    return linon_user::field_function(pv, pp, p, v0, v, t);
+  }
+};
+)LINON";
+  s << "extern \"C\" __global__ void LINON_MARCH_BOUNDS " << march_kernel_name(v)
+    << "(linon::MarchArgs a) {\n  linon::march_pair_kernel<" << (v & ~16) << ">(LinonFieldPair(), a);\n}\n";
+  return s.str();
+}
+
 std::vector<std::string> module_kernels(const std::vector<int>& variants, bool base) {
   std::vector<std::string> k;
   for (int v : variants) k.push_back(march_kernel_name(v));
@@ -236,7 +255,8 @@ int march_kernel(const linon_field* f, int v, cudaKernel_t* out) {
     std::shared_ptr<JitModule> mod;
     std::string log;
     const bool precise = (f->flags & LINON_COMPILE_PRECISE) != 0;
-    int st = jit_compile(module_source(f->cuda, {v}, false), precise, module_kernels({v}, false), mod, log);
+    const std::string src = (v & 16) ? module_source_pair(f->cuda_pair, v) : module_source(f->cuda, {v}, false);
+    int st = jit_compile(src, precise, module_kernels({v}, false), mod, log);
     if (st != LINON_OK) return set_error(st, st == LINON_ECOMPILE ? log : std::string(g_last_error));
     vit = f->variants.emplace(v, mod).first;
   }
@@ -595,6 +615,15 @@ int linon_field_validate(const char* field_body, const char* helpers_src, int fl
     st = jit_check(batched_module_source({&tmp}), precise, blog, &bytes);
     jlog += blog;
   }
+  if (st == LINON_OK && !precise) {
+    // the pair form (two rays per thread), when the field has one: its
+    // absence or a compile failure only means one ray per thread
+    wgslfe::Translation tp = wgslfe::translate(field_body, helpers_src ? helpers_src : "", "linon_user", true);
+    std::string plog;
+    size_t pbytes = 0;
+    const int pst = tp.ok ? jit_check(module_source_pair(tp.code, 14 | 16), false, plog, &pbytes) : LINON_ECOMPILE;
+    jlog += pst == LINON_OK ? "\npair form: compiles\n" + plog : "\npair form: not available\n";
+  }
   copy_log(jlog, log, log_cap);
   if (st != LINON_OK) return set_error(st, jlog);
   return LINON_OK;
@@ -627,6 +656,10 @@ int linon_field_compile(linon_ctx* ctx, const char* field_body, const char* help
   f->body = field_body;
   f->helpers = helpers_src ? helpers_src : "";
   f->cuda = t.code;
+  if (!precise) {
+    wgslfe::Translation tp = wgslfe::translate(field_body, helpers_src ? helpers_src : "", "linon_user", true);
+    if (tp.ok) f->cuda_pair = tp.code;
+  }
   f->stateful = t.has_private;
   f->flags = flags;
   f->flops_arith = t.flops_arith;
@@ -643,6 +676,12 @@ int linon_field_release(linon_ctx* ctx, linon_field* field) {
   if (field->ctx != ctx) return set_error(LINON_EINVAL, "field belongs to another context");
   delete field;  // the compiled module stays cached for the process
   return LINON_OK;
+}
+
+int linon_field_pair_state(const linon_field* field) {
+  if (!field) return -1;
+  if (field->cuda_pair.empty()) return -1;
+  return field->pair_state;
 }
 
 int linon_field_flops(const linon_field* field, int32_t* arith, int32_t* transcendental) {
@@ -691,10 +730,27 @@ int launch_rows(linon_ctx* ctx, const linon_field* field, const linon_camera* ca
   a.err = ctx->d_err;
   cudaKernel_t k;
   const bool precise = (field->flags & LINON_COMPILE_PRECISE) != 0;
-  if (int st = march_kernel(field, march_variant(params, settings, precise), &k)) return st;
+  const int v = march_variant(params, settings, precise);
+  // Fixed step budgets without adaptive retries, early stop or linear mode
+  // run two rays per thread when the field has a pair form that compiles
+  // (the first such render compiles it; a field that does not compile in
+  // pair form keeps the one-ray kernel).  LINON_NO_PAIRS turns this off.
+  bool pairs = !precise && (v & 4) && !(v & 1) && !params->stop_on_hit && !params->linear_mode &&
+               !field->cuda_pair.empty() && field->pair_state >= 0 && !std::getenv("LINON_NO_PAIRS");
+  if (pairs) {
+    if (march_kernel(field, v | 16, &k) == LINON_OK) {
+      field->pair_state = 1;
+      a.tile_w = 16;
+    } else {
+      field->pair_state = -1;
+      pairs = false;
+    }
+  }
+  if (!pairs)
+    if (int st = march_kernel(field, v, &k)) return st;
   dim3 grid((out->width + a.tile_w - 1) / a.tile_w, (row1 - row0 + a.tile_h - 1) / a.tile_h);
   void* args[] = {&a};
-  LINON_CUDA(cudaLaunchKernel((const void*)k, grid, dim3(a.tile_w * a.tile_h), args,
+  LINON_CUDA(cudaLaunchKernel((const void*)k, grid, dim3((pairs ? a.tile_w / 2 : a.tile_w) * a.tile_h), args,
                               size_t(a.scene.staged_bytes), stream));
   return LINON_OK;
 }

@@ -116,6 +116,8 @@ struct linon_field {
   int flags = 0;
   int flops_arith = 0, flops_transc = 0;
   bool stateful = false;  // var<private> state: batches use the one-CTA-per-tile schedule
+  std::string cuda_pair;  // the field in pair form (two rays per thread), "" if none
+  mutable int pair_state = 0;  // pair kernels: 0 not tried, 1 compiled, -1 not available
   std::shared_ptr<linon::JitModule> mod;  // capture, field_eval, base march variant
   mutable std::mutex vmu;                  // guards `variants`
   mutable std::map<int, std::shared_ptr<linon::JitModule>> variants;  // other march variants

@@ -147,12 +147,20 @@ std::string wgsl_name(const Ty& t) {
   }
   return "?";
 }
+// Pair emission (translate(..., pair = true)): every f32 value becomes a
+// ::wgsl::f2, the same value of two rays, so that one thread evaluates the
+// field for two rays with packed FP32 pair instructions.  Literals stay
+// float (they broadcast); anything that is not lane-wise in an f2 (a
+// comparison, a branch on a value, a conversion to an integer) has no f2
+// overload and fails to compile, and the engine then uses the one-ray
+// kernels.
+thread_local bool g_pair = false;
 const char* sk_cpp(SK s) {
   switch (s) {
     case SK::Bool: return "bool";
     case SK::I32: case SK::AInt: return "int";
     case SK::U32: return "unsigned";
-    case SK::F32: case SK::AFloat: return "float";
+    case SK::F32: case SK::AFloat: return g_pair ? "::wgsl::f2" : "float";
   }
   return "?";
 }
@@ -2998,7 +3006,12 @@ int count_lines(const std::string& s) {
 }  // namespace
 
 Translation translate(const std::string& field_body, const std::string& helpers_src,
-                      const std::string& ns) {
+                      const std::string& ns, bool pair) {
+  struct PairScope {
+    bool old;
+    explicit PairScope(bool on) : old(g_pair) { g_pair = on; }
+    ~PairScope() { g_pair = old; }
+  } pair_scope(pair);
   Translation tr;
   // The module the reference builds: the shader's helpers followed by the
   // spliced field function (main_view.rs:852-861).  User helpers take the

@@ -28,9 +28,12 @@ struct Translation {
 // ns::field_function(ns::Private& pv, vec3f p_prev, vec3f p, vec3f v0,
 // vec3f v, float t), where ns::Private holds the module's var<private>
 // variables (an empty struct when there are none): one Private per
-// invocation, i.e. per ray.
+// invocation, i.e. per ray.  pair = true emits the same functions with every
+// f32 value a ::wgsl::f2 (two rays' values, evaluated with packed FP32
+// pairs; see device/wgsl_rt.cuh): field_function(Private&, vec<f2,3> p_prev,
+// vec<f2,3> p, vec<f2,3> v0, vec<f2,3> v, f2 t).
 Translation translate(const std::string& field_body, const std::string& helpers_src,
-                      const std::string& ns);
+                      const std::string& ns, bool pair = false);
 
 }  // namespace wgslfe
 }  // namespace linon

@@ -72,6 +72,11 @@ class Field:
         check(load().linon_field_flops(self.handle, C.byref(a), C.byref(t)))
         return a.value, t.value
 
+    def pair_state(self) -> int:
+        """linon_field_pair_state: 1 fixed-step renders run two rays per
+        thread, 0 not tried yet, -1 one ray per thread."""
+        return int(load().linon_field_pair_state(self.handle))
+
     def cuda_source(self) -> str:
         return load().linon_field_cuda_source(self.handle).decode()
 

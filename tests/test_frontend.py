@@ -1362,3 +1362,26 @@ def test_helper_calls_the_field_function():
     with pytest.raises(_abi.LinonCompileError) as e:
         translate_wgsl("return euler(p, v, 0.1);", CALLER_HELPERS)
     assert "recursion" in str(e.value)
+
+
+@pytest.mark.parametrize("name,has_pair", [("linear", True), ("twist", True), ("lens", True), ("lorenz_scaled", True),
+                                           ("rotation", True), ("translation_x", True), ("lorenz", True),
+                                           ("mirage_spherical", False), ("mirage_plane_sigmoid", False)])
+def test_pair_form_of_the_predefined_fields(name, has_pair):
+    """Fields whose arithmetic is lane-wise compile in pair form (two rays
+    per thread, packed FP32 pairs) for sm_103a; fields that branch on a value
+    (the mirages' refraction) have none and keep one ray per thread."""
+    from linon_gb300 import _abi
+    from linon_gb300.engine import predefined_source, validate_field
+    log = validate_field(predefined_source(_abi.FIELD_IDS[name]))
+    assert ("pair form: compiles" in log) == has_pair, log[-400:]
+    assert ("pair form: not available" in log) == (not has_pair)
+
+
+def test_pair_form_rejects_a_branch_on_a_value():
+    from linon_gb300.engine import validate_field
+    log = validate_field("if (p.x < 0.0) { return v; }\nreturn v0;")
+    assert "pair form: not available" in log
+    # precise modules have no pair form at all
+    log = validate_field("return v0;", precise=True)
+    assert "pair form" not in log

@@ -681,3 +681,43 @@ def test_main_view_mirror(engine):
     torch.cuda.synchronize()
     assert pos.shape == (8, 2)
     assert mv.texture.shape == (48, 64, 4)
+
+
+@pytest.mark.parametrize("name", ["linear", "twist", "lens", "lorenz_scaled"])
+def test_pair_kernel_matches_one_ray_kernel(engine, name, monkeypatch):
+    """Two rays per thread (fixed step budget, fast module) against one ray
+    per thread on the same frame: an odd width (the last pixel pair has one
+    lane outside the image) and a band of rows (linon_render_rows).  The two
+    kernels round every operation alike except where the one-ray kernel's
+    compiler contracts a multiply-add differently from the pair kernel's
+    explicit packed FMAs, so endpoints agree to FP32 rounding (smooth fields
+    within 1e-4 at the 99.9th percentile; the chaotic lens orbits at the
+    median) and hit ids and colours agree except on rounding ties."""
+    w = wl.frames_1080p(241, 135)
+    w.params = wl.fixed_steps(0.005, 800, kahan=True)
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    fld = engine.compile_field(predefined_source(_abi.FIELD_IDS[name]))
+    monkeypatch.delenv("LINON_NO_PAIRS", raising=False)
+    g2 = gpu_render(engine, w, fld)
+    assert fld.pair_state() == 1
+    monkeypatch.setenv("LINON_NO_PAIRS", "1")
+    g1 = gpu_render(engine, w, fld)
+    monkeypatch.delenv("LINON_NO_PAIRS")
+    assert (g2["steps"] == 800).all() and (g1["steps"] == 800).all()
+    same = g2["hit_id"] == g1["hit_id"]
+    assert same.mean() >= 0.995, same.mean()
+    d = np.linalg.norm(g2["mapping"][..., :3].astype(np.float64) - g1["mapping"][..., :3], axis=-1)
+    if name == "lens":
+        assert np.median(d) <= 1e-4, np.median(d)
+    else:
+        assert np.percentile(d, 99.9) <= 1e-4, np.percentile(d, 99.9)
+    dc = np.abs(g2["color"].astype(int) - g1["color"].astype(int))[same].max()
+    assert dc <= 1, dc
+    assert (g2["color"][..., 3] == 255).all()
+    # a band of rows gives the whole frame's rows bit for bit
+    band = FramePlanes.allocate(w.width, w.height)
+    engine.render_rows(fld, w.camera, w.settings, w.params, band, 37, 101)
+    torch.cuda.synchronize()
+    engine.synchronize()
+    for k in ("color", "mapping", "hit_id", "steps"):
+        np.testing.assert_array_equal(getattr(band, k).cpu().numpy()[37:101], g2[k][37:101], err_msg=k)
