@@ -124,6 +124,17 @@ def flops_per_step(pyoracle, w, fid):
     return float(live[:, :4].sum(axis=1).mean()), float(live[:, 4].mean())
 
 
+def kernel_name(field, label):
+    """The march kernel a 1080p frame of `field` runs: two rays per thread
+    (v30) when the field has a compiled pair form and at least 14 FP32
+    operations and at most one transcendental per evaluation (the engine's
+    rule; 1080p frames fill the GPU), else one ray per thread (v14)."""
+    arith, transc = field.flops()
+    pairs = field.pair_state() == 1 and arith >= 14 and transc <= 1
+    return (f"linon_march_v{30 if pairs else 14} ({label} field; fixed steps, Kahan, field_weight 1; "
+            f"{'two rays' if pairs else 'one ray'} per thread)")
+
+
 def cpu_baseline(pyoracle, w, budget_s=12.0):
     """The oracle (FP32 restatement) on the host cores over a stratified
     pixel sample of the same frames; returns ray-steps/s and the sample."""
@@ -367,8 +378,7 @@ def main():
                               "frac": achieved / peak, "traffic": None,
                               "traffic_note": "DRAM bytes per launch are in profiles/ (ncu); the 58 MB of "
                                               "output planes are still L2-resident when the launch ends",
-                              "kernel": f"linon_march_v14 ({['linear', 'twist', 'lens'][i]} field; "
-                                        "fixed steps, Kahan, field_weight 1)",
+                              "kernel": kernel_name(fields[i], ["linear", "twist", "lens"][i]),
                               "peak_source": "measured FFMA probe in this run (linon_probe_fp32_peak)",
                               "peak_nominal_at_median_clock": (n_sm * 128 * 2 * clk["sm_mhz"] * 1e6 / 1e12
                                                                if clk.get("sm_mhz") else None),

@@ -731,16 +731,37 @@ int launch_rows(linon_ctx* ctx, const linon_field* field, const linon_camera* ca
   cudaKernel_t k;
   const bool precise = (field->flags & LINON_COMPILE_PRECISE) != 0;
   const int v = march_variant(params, settings, precise);
-  // Fixed step budgets without adaptive retries, early stop or linear mode
-  // run two rays per thread when the field has a pair form that compiles
-  // (the first such render compiles it; a field that does not compile in
-  // pair form keeps the one-ray kernel).  LINON_NO_PAIRS turns this off.
+  // Two rays per thread (march_pair_kernel) for fixed step budgets without
+  // adaptive retries, early stop or linear mode, when the field has a pair
+  // form that compiles (the first such render compiles it).  Pairs halve
+  // the FP32 issue of the field and the step but leave the FMA pipe's work
+  // as it is and hold more registers (fewer warps per SM, CTAs with twice
+  // the work), so they pay only where the field's arithmetic dominates the
+  // step and the frame fills the GPU many times over: measured at 1080p x
+  // 4000 steps, lens (24 operations and one transcendental per evaluation)
+  // 29.2 -> 28.1 ms and the scaled Lorenz field (14, 0) 21.1 -> 20.3 ms, but
+  // twist (16 and a sine and cosine) 19.5 -> 21.0 ms, linear (0) 6.3 -> 8.7
+  // ms, and the Lorenz field at 1024^2 (4.5 waves of pair CTAs) 7.4 -> 8.5
+  // ms.  Rule: at least 14 FP32 operations and at most one transcendental
+  // per evaluation, and at least 8 waves of the pair kernel's resident CTAs.
+  // LINON_RAY_PAIRS=0 / =1 forces one ray / two rays per thread.
+  const char* force = std::getenv("LINON_RAY_PAIRS");
   bool pairs = !precise && (v & 4) && !(v & 1) && !params->stop_on_hit && !params->linear_mode &&
-               !field->cuda_pair.empty() && field->pair_state >= 0 && !std::getenv("LINON_NO_PAIRS");
+               !field->cuda_pair.empty() && field->pair_state >= 0 && !(force && force[0] == '0');
+  if (pairs && !(force && force[0] == '1'))
+    pairs = field->flops_arith >= 14 && field->flops_transc <= 1;
   if (pairs) {
     if (march_kernel(field, v | 16, &k) == LINON_OK) {
       field->pair_state = 1;
-      a.tile_w = 16;
+      if (!(force && force[0] == '1')) {
+        int occ = 0, sms = 0;
+        LINON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)k, 128,
+                                                                 size_t(a.scene.staged_bytes)));
+        LINON_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+        const long long ctas = (long long)((out->width + 15) / 16) * ((row1 - row0 + 15) / 16);
+        pairs = ctas >= 8LL * sms * std::max(occ, 1);
+      }
+      if (pairs) a.tile_w = 16;
     } else {
       field->pair_state = -1;
       pairs = false;

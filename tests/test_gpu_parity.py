@@ -697,12 +697,12 @@ def test_pair_kernel_matches_one_ray_kernel(engine, name, monkeypatch):
     w.params = wl.fixed_steps(0.005, 800, kahan=True)
     engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
     fld = engine.compile_field(predefined_source(_abi.FIELD_IDS[name]))
-    monkeypatch.delenv("LINON_NO_PAIRS", raising=False)
+    monkeypatch.setenv("LINON_RAY_PAIRS", "1")
     g2 = gpu_render(engine, w, fld)
     assert fld.pair_state() == 1
-    monkeypatch.setenv("LINON_NO_PAIRS", "1")
+    monkeypatch.setenv("LINON_RAY_PAIRS", "0")
     g1 = gpu_render(engine, w, fld)
-    monkeypatch.delenv("LINON_NO_PAIRS")
+    monkeypatch.setenv("LINON_RAY_PAIRS", "1")
     assert (g2["steps"] == 800).all() and (g1["steps"] == 800).all()
     same = g2["hit_id"] == g1["hit_id"]
     assert same.mean() >= 0.995, same.mean()
@@ -719,5 +719,6 @@ def test_pair_kernel_matches_one_ray_kernel(engine, name, monkeypatch):
     engine.render_rows(fld, w.camera, w.settings, w.params, band, 37, 101)
     torch.cuda.synchronize()
     engine.synchronize()
+    monkeypatch.delenv("LINON_RAY_PAIRS")
     for k in ("color", "mapping", "hit_id", "steps"):
         np.testing.assert_array_equal(getattr(band, k).cpu().numpy()[37:101], g2[k][37:101], err_msg=k)
