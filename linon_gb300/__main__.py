@@ -3,6 +3,7 @@
     python -m linon_gb300 render --workload frames_1080p --field twist \
         --width 480 --height 270 --repeat 2 [--precise] [--brute-force]
     python -m linon_gb300 batch --views 64 --repeat 2 [--plain]
+    python -m linon_gb300 lyapunov --width 1024 --height 1024 --repeat 2
     python -m linon_gb300 validate --field lens        # NVRTC report, no GPU
 
 Prints one JSON line with the device time per launch (CUDA events).
@@ -89,6 +90,27 @@ def cmd_batch(a):
     eng.close()
 
 
+def cmd_lyapunov(a):
+    """The Lyapunov pipeline (render, FP64 overlay, finite-time exponent,
+    quantile threshold, outline pixels, outline capture) of the 1024^2
+    workload at the given size; per-stage device ms."""
+    import torch
+    from . import lyapunov
+    w = wl.lyapunov_1024(a.width, a.height)
+    eng = Engine(0)
+    stream = torch.cuda.Stream()
+    eng.set_stream(stream)
+    eng.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    fld = eng.compile_field(predefined_source(w.fields[0]))
+    runs = []
+    with torch.cuda.stream(stream):
+        for _ in range(a.repeat):
+            runs.append(lyapunov.run(eng, fld, w, horizon=w.extra["T"], quantile=w.extra["quantile"], timings=True))
+    print(json.dumps({"workload": w.name, "width": w.width, "height": w.height,
+                      "ms": [r["ms"] for r in runs], "threshold": runs[-1]["threshold"]}))
+    eng.close()
+
+
 def cmd_validate(a):
     print(validate_field(predefined_source(_field_id(a.field)), precise=a.precise))
 
@@ -115,11 +137,15 @@ def main():
     b.add_argument("--refill-below", type=int, default=0,
                    help="persistent queue: refill a warp's free lanes once fewer than this many are marching")
     b.add_argument("--block-threads", type=int, default=128, help="persistent queue: threads per CTA")
+    ly = sub.add_parser("lyapunov")
+    ly.add_argument("--width", type=int, default=1024)
+    ly.add_argument("--height", type=int, default=1024)
+    ly.add_argument("--repeat", type=int, default=2)
     v = sub.add_parser("validate")
     v.add_argument("--field", default="twist")
     v.add_argument("--precise", action="store_true")
     a = ap.parse_args()
-    {"render": cmd_render, "batch": cmd_batch, "validate": cmd_validate}[a.cmd](a)
+    {"render": cmd_render, "batch": cmd_batch, "lyapunov": cmd_lyapunov, "validate": cmd_validate}[a.cmd](a)
 
 
 if __name__ == "__main__":
