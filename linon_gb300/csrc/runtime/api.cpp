@@ -621,7 +621,8 @@ int linon_field_validate(const char* field_body, const char* helpers_src, int fl
     wgslfe::Translation tp = wgslfe::translate(field_body, helpers_src ? helpers_src : "", "linon_user", true);
     std::string plog;
     size_t pbytes = 0;
-    const int pst = tp.ok ? jit_check(module_source_pair(tp.code, 14 | 16), false, plog, &pbytes) : LINON_ECOMPILE;
+    const int pst = tp.ok && !tp.has_private ? jit_check(module_source_pair(tp.code, 14 | 16), false, plog, &pbytes)
+                                             : LINON_ECOMPILE;
     jlog += pst == LINON_OK ? "\npair form: compiles\n" + plog : "\npair form: not available\n";
   }
   copy_log(jlog, log, log_cap);
@@ -656,7 +657,9 @@ int linon_field_compile(linon_ctx* ctx, const char* field_body, const char* help
   f->body = field_body;
   f->helpers = helpers_src ? helpers_src : "";
   f->cuda = t.code;
-  if (!precise) {
+  // no pair form with var<private> state: an integer or boolean private
+  // variable would be one value for both rays of a thread
+  if (!precise && !t.has_private) {
     wgslfe::Translation tp = wgslfe::translate(field_body, helpers_src ? helpers_src : "", "linon_user", true);
     if (tp.ok) f->cuda_pair = tp.code;
   }

@@ -31,7 +31,10 @@ struct Translation {
 // invocation, i.e. per ray.  pair = true emits the same functions with every
 // f32 value a ::wgsl::f2 (two rays' values, evaluated with packed FP32
 // pairs; see device/wgsl_rt.cuh): field_function(Private&, vec<f2,3> p_prev,
-// vec<f2,3> p, vec<f2,3> v0, vec<f2,3> v, f2 t).
+// vec<f2,3> p, vec<f2,3> v0, vec<f2,3> v, f2 t).  Integer and boolean values
+// stay scalar in pair form, which is right for values that cannot depend on
+// the ray (no f2 converts to them) but not for var<private> state, so the
+// engine gives fields with private state no pair form.
 Translation translate(const std::string& field_body, const std::string& helpers_src,
                       const std::string& ns, bool pair = false);
 

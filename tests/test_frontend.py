@@ -1385,3 +1385,7 @@ def test_pair_form_rejects_a_branch_on_a_value():
     # precise modules have no pair form at all
     log = validate_field("return v0;", precise=True)
     assert "pair form" not in log
+    # nor fields with var<private> state: a private integer would be one
+    # value for both rays of a thread
+    log = validate_field("count = count + 1;\nreturn v0 * f32(count);", helpers="var<private> count: i32;")
+    assert "pair form: not available" in log
