@@ -746,7 +746,8 @@ int launch_rows(linon_ctx* ctx, const linon_field* field, const linon_camera* ca
   // twist (16 and a sine and cosine) 19.5 -> 21.0 ms, linear (0) 6.3 -> 8.7
   // ms, and the Lorenz field at 1024^2 (4.5 waves of pair CTAs) 7.4 -> 8.5
   // ms.  Rule: at least 14 FP32 operations and at most one transcendental
-  // per evaluation, and at least 8 waves of the pair kernel's resident CTAs.
+  // per evaluation, and a frame of at least 8 waves of the pair kernel's
+  // resident CTAs.
   // LINON_RAY_PAIRS=0 / =1 forces one ray / two rays per thread.
   const char* force = std::getenv("LINON_RAY_PAIRS");
   bool pairs = !precise && (v & 4) && !(v & 1) && !params->stop_on_hit && !params->linear_mode &&
@@ -761,7 +762,9 @@ int launch_rows(linon_ctx* ctx, const linon_field* field, const linon_camera* ca
         LINON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)k, 128,
                                                                  size_t(a.scene.staged_bytes)));
         LINON_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
-        const long long ctas = (long long)((out->width + 15) / 16) * ((row1 - row0 + 15) / 16);
+        // the whole frame's CTAs: row bands of one frame (linon_render_host)
+        // are launched back to back on two streams and overlap
+        const long long ctas = (long long)((out->width + 15) / 16) * ((out->height + 15) / 16);
         pairs = ctas >= 8LL * sms * std::max(occ, 1);
       }
       if (pairs) a.tile_w = 16;
