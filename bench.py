@@ -545,8 +545,8 @@ def bench_batch(eng, stream, wl, torch, dev, predefined_source, keep=None):
 
     plain_ms = timed(lambda: eng.render_views_plain(flds, views))
     steps_plain = sum(int(p.steps.sum().item()) for p in planes)
-    # the persistent work-queue form on its own (quantum 1024, 128-thread
-    # CTAs, 4x8-ray tiles, refill when the warp is empty)
+    # the persistent work-queue form on its own (each warp takes whole
+    # 4x8-pixel tiles of 32 rays; 128-thread CTAs)
     pq = _abi.BatchTuning(1024, 128, 0, 4, 8, 0, 1)
     persistent_ms = timed(lambda: eng.render_batch(flds, views, pq))
     tuning, tune_ms = eng.autotune_batch(flds, views)
@@ -560,9 +560,10 @@ def bench_batch(eng, stream, wl, torch, dev, predefined_source, keep=None):
             "batched_ms": batch_ms, "plain_ray_steps_per_s": steps_plain / (plain_ms * 1e-3),
             "batched_ray_steps_per_s": steps_batch / (batch_ms * 1e-3), "speedup": plain_ms / batch_ms,
             "persistent_queue": {"ms": persistent_ms, "speedup": plain_ms / persistent_ms,
-                                 "tuning": {"quantum": 1024, "block_threads": 128, "tile": [4, 8],
-                                            "refill_below": 0}},
-            "tuning": {"schedule": {1: "persistent queue", 2: "one CTA per tile"}.get(tuning.schedule, "auto"),
+                                 "tuning": {"form": "warps take whole tiles", "block_threads": 128,
+                                            "tile": [4, 8], "refill_below": 0}},
+            "tuning": {"schedule": {1: "persistent queue" + (" (lane refills)" if tuning.refill_below else ""),
+                                    2: "one CTA per tile"}.get(tuning.schedule, "auto"),
                        "quantum": tuning.quantum, "block_threads": tuning.block_threads,
                        "tile": [tuning.tile_w, tuning.tile_h], "refill_below": tuning.refill_below}}
 

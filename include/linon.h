@@ -356,17 +356,21 @@ int linon_outline_indices(uint16_t* out, size_t cap);
  * Views of any size, camera, step size and field go into one launch, in
  * one of two schedules: one CTA per 8x16-pixel tile of every view, views
  * with the largest step budget first, the hardware balancing the CTAs (the
- * default); or a persistent kernel over a device work queue of ray tiles
- * whose warps retire finished rays and refill from the queue every
- * `quantum` steps.  fields[] may hold up to LINON_MAX_BATCH_FIELDS
- * distinct fields; views[i].field_index selects.                           */
+ * default); or a persistent kernel over a device work queue of 32-ray
+ * tiles (views with the largest step budget first) whose warps each march
+ * a whole tile and take the next (refill_below = 0), or retire finished
+ * rays and refill free lanes every `quantum` steps once fewer than
+ * refill_below lanes march.  fields[] may hold up to
+ * LINON_MAX_BATCH_FIELDS distinct fields; views[i].field_index selects.   */
 #define LINON_MAX_BATCH_FIELDS 8
 typedef struct linon_batch_tuning {
-  int32_t quantum;          /* RK4 steps between retire/refill (0 = auto)  */
+  int32_t quantum;          /* lane refills: RK4 steps between retire/refill
+                               (0 = auto)                                   */
   int32_t block_threads;    /* threads per CTA (0 = auto)                  */
   int32_t ctas_per_sm;      /* resident CTAs per SM (0 = auto)             */
   int32_t tile_w, tile_h;   /* pixel tile handed out per queue pop (0=auto) */
-  int32_t refill_below;     /* refill early when fewer lanes march (0=auto) */
+  int32_t refill_below;     /* 0: warps take whole tiles; > 0: refill free
+                               lanes once fewer than this many march        */
   int32_t schedule;         /* 0 auto (= 2), 1 persistent queue (the
                                fields above), 2 one CTA per 8x16-pixel tile
                                of every view (hardware scheduling)          */

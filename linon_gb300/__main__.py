@@ -74,7 +74,8 @@ def cmd_batch(a):
         if a.plain:
             eng.render_views_plain(flds, views)
         elif a.schedule == 1:
-            eng.render_batch(flds, views, _abi.BatchTuning(a.quantum, a.block_threads, 0, 4, 8, a.refill_below, 1))
+            eng.render_batch(flds, views, _abi.BatchTuning(a.quantum, a.block_threads, a.ctas_per_sm, a.tile[0], a.tile[1],
+                                                           a.refill_below, 1))
         elif a.schedule == 2:
             eng.render_batch(flds, views, _abi.BatchTuning(0, 0, 0, 0, 0, 0, 2))
         else:
@@ -85,7 +86,7 @@ def cmd_batch(a):
         ts.append(s.elapsed_time(e))
     steps = sum(int(p.steps.sum().item()) for p in planes)
     print(json.dumps({"views": len(views), "plain": a.plain, "schedule": a.schedule, "quantum": a.quantum,
-                      "refill_below": a.refill_below, "block_threads": a.block_threads, "ms": ts, "ray_steps": steps,
+                      "refill_below": a.refill_below, "block_threads": a.block_threads, "tile": list(a.tile), "ms": ts, "ray_steps": steps,
                       "ray_steps_per_s": steps / (statistics.median(ts) * 1e-3)}))
     eng.close()
 
@@ -137,6 +138,9 @@ def main():
     b.add_argument("--refill-below", type=int, default=0,
                    help="persistent queue: refill a warp's free lanes once fewer than this many are marching")
     b.add_argument("--block-threads", type=int, default=128, help="persistent queue: threads per CTA")
+    b.add_argument("--ctas-per-sm", type=int, default=0, help="persistent queue: resident CTAs per SM (0 = most)")
+    b.add_argument("--tile", type=int, nargs=2, default=(4, 8), metavar=("W", "H"),
+                   help="persistent queue: pixel tile of 32 rays a warp takes")
     ly = sub.add_parser("lyapunov")
     ly.add_argument("--width", type=int, default=1024)
     ly.add_argument("--height", type=int, default=1024)

@@ -114,8 +114,8 @@ __device__ __forceinline__ bool box_overlap(const float4& lo, const float4& hi, 
 
 // Launch bounds of the persistent batched kernels: up to 256-thread CTAs,
 // at least LINON_BATCH_MIN_CTAS (default 4) of them resident per SM, which
-// caps the kernels at 64 registers (64 uneven views, quantum 1024: 13.5 ms
-// uncapped at 80 registers, 13.3 ms at 4 CTAs, 13.6 ms at 3).
+// caps the kernels at 64 registers (64 uneven views, warps taking whole
+// tiles: 11.55 ms at 4, 11.73 ms at 3 (80 registers), 14.1 ms at 5).
 #ifndef LINON_BATCH_MIN_CTAS
 #define LINON_BATCH_MIN_CTAS 4
 #endif
@@ -954,6 +954,22 @@ __device__ __forceinline__ void march_pair_kernel(const F& field, const MarchArg
 // counter[0] holds the first view that may still have rays).  Warps exit
 // when every view is drained and their lanes are done.
 // --------------------------------------------------------------------------
+// linear_mode's one straight segment per pixel (main_view.wgsl:368-370).
+__device__ __forceinline__ void linear_shot(const SceneView& sc, const vec3f& origin, const vec3f& dir,
+                                            const DevFrame& out, size_t idx, int* err) {
+  HitRec hit = intersect_segment<true>(sc, origin, dir, 100.0f, origin + 100.0f * dir, err);
+  wgsl::vec4f c(0.0f, 0.0f, 0.0f, 0.0f);
+  if (hit.t > 0.0f && hit.t < 100.0f) c = shade_hit(sc, hit, dir);
+  if (out.color) {
+    uchar4 o;
+    o.x = unorm8(c.x); o.y = unorm8(c.y); o.z = unorm8(c.z); o.w = unorm8(c.w);
+    out.color[idx] = o;
+  }
+  if (out.hit) out.hit[idx] = hit.t > 0.0f && hit.t < 100.0f ? hit.id : -1;
+  if (out.mapping) out.mapping[idx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (out.steps) out.steps[idx] = 0;
+}
+
 template <class F>
 __device__ __forceinline__ void ray_step_rt(RayState& r, const F& field, const DevMarch& m,
                                             const SceneView& sc, int* err) {
@@ -1044,18 +1060,7 @@ __device__ __forceinline__ void march_batch_kernel(const Fields& fields, const B
             ray_init(r, wb.origin, primary_dir(wb, x, V.frame.H - 1 - row), m.h_initial);
             active = true;
             if (m.linear_mode) {
-              HitRec hit = intersect_segment<true>(sc, wb.origin, r.dir, 100.0f, wb.origin + 100.0f * r.dir, a.err);
-              wgsl::vec4f c(0.0f, 0.0f, 0.0f, 0.0f);
-              if (hit.t > 0.0f && hit.t < 100.0f) c = shade_hit(sc, hit, r.dir);
-              const DevFrame& out = V.frame;
-              if (out.color) {
-                uchar4 o;
-                o.x = unorm8(c.x); o.y = unorm8(c.y); o.z = unorm8(c.z); o.w = unorm8(c.w);
-                out.color[pix] = o;
-              }
-              if (out.hit) out.hit[pix] = hit.t > 0.0f && hit.t < 100.0f ? hit.id : -1;
-              if (out.mapping) out.mapping[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-              if (out.steps) out.steps[pix] = 0;
+              linear_shot(sc, wb.origin, r.dir, V.frame, pix, a.err);
               active = false;
             }
           }
@@ -1082,6 +1087,73 @@ __device__ __forceinline__ void march_batch_kernel(const Fields& fields, const B
       ray_store(r, V.frame, pix);
       active = false;
     }
+  }
+}
+
+// Persistent queue of ray tiles, one tile per warp: a warp takes the next
+// tile_w x tile_h tile of 32 rays from the first view that has tiles left
+// (views with the largest step budget first), marches it to the end with the
+// plain kernel's loop (per-step warp vote) and takes the next.  Unlike the
+// lane-refilling queue above no lane carries queue state through the march,
+// and unlike one CTA per tile a warp whose rays end early does not wait for
+// the other warps of its CTA: it takes the next tile at once.
+__device__ __forceinline__ int take_tile(const BatchArgs& a, unsigned long long& base) {
+  int v = int(*(volatile unsigned long long*)a.counter);
+  for (; v < a.n_views; ++v) {
+    const long long n = view_rays(a, v);
+    if ((long long)*(volatile unsigned long long*)&a.views[v].next < n) {
+      const unsigned long long b = atomicAdd(&a.views[v].next, 32ull);
+      if ((long long)b < n) {
+        base = b;
+        return v;
+      }
+    }
+    atomicMax(a.counter, (unsigned long long)(v + 1));  // view v is drained
+  }
+  return -1;
+}
+
+template <int MODE = 0, class Fields>
+__device__ __forceinline__ void march_queue_kernel(const Fields& fields, const BatchArgs& a) {
+  extern __shared__ float4 linon_smem[];
+  __shared__ unsigned long long mbar;
+  const SceneView sc = cta_scene(a.scene, linon_smem, &mbar, a.err);
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned long long base = 0;
+    int view = 0;
+    if (lane == 0) view = take_tile(a, base);
+    view = __shfl_sync(FULL, view, 0);
+    if (view < 0) break;
+    base = __shfl_sync(FULL, base, 0);
+    const BatchView& V = a.views[view];
+    const int tile = int(base >> 5);  // ray_begin and the queue advance in whole tiles of 32
+    const int x = (tile % V.tiles_x) * a.tile_w + lane % a.tile_w;
+    const int row = (tile / V.tiles_x) * a.tile_h + lane / a.tile_w;
+    const int W = V.frame.W, H = V.frame.H;
+    const bool in_image = x < W && row < H;
+    const DevMarch m = V.m;
+    const Basis b = make_basis(V.cam, W, H, m.focal_length, m.viewport_height);
+    const vec3f dir = primary_dir(b, in_image ? x : 0, in_image ? H - 1 - row : 0);
+    const size_t idx = in_image ? size_t(row) * W + x : 0;
+    RayState r;
+    ray_init(r, b.origin, dir, m.h_initial);
+    if (m.linear_mode) {
+      if (in_image) linear_shot(sc, b.origin, dir, V.frame, idx, a.err);
+      continue;
+    }
+    fields.visit(V.field, [&](const auto& field) {
+      bool active = in_image && ray_active(r, m);
+      while (__any_sync(FULL, active)) {
+        if (active) {
+          if (MODE == 0) ray_step_rt(r, field, m, sc, a.err);
+          else ray_step<false, MODE == 2, false, true>(r, field, m, sc, a.err);
+          active = ray_active(r, m);
+        }
+      }
+    });
+    if (in_image) ray_store(r, V.frame, idx);
   }
 }
 
@@ -1119,19 +1191,7 @@ __device__ __forceinline__ void march_multi_kernel(const Fields& fields, const B
   RayState r;
   ray_init(r, b.origin, dir, m.h_initial);
   if (m.linear_mode) {
-    if (!in_image) return;
-    HitRec hit = intersect_segment<true>(sc, b.origin, dir, 100.0f, b.origin + 100.0f * dir, a.err);
-    wgsl::vec4f c(0.0f, 0.0f, 0.0f, 0.0f);
-    if (hit.t > 0.0f && hit.t < 100.0f) c = shade_hit(sc, hit, dir);
-    const DevFrame& out = V.frame;
-    if (out.color) {
-      uchar4 o;
-      o.x = unorm8(c.x); o.y = unorm8(c.y); o.z = unorm8(c.z); o.w = unorm8(c.w);
-      out.color[idx] = o;
-    }
-    if (out.hit) out.hit[idx] = hit.t > 0.0f && hit.t < 100.0f ? hit.id : -1;
-    if (out.mapping) out.mapping[idx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (out.steps) out.steps[idx] = 0;
+    if (in_image) linear_shot(sc, b.origin, dir, V.frame, idx, a.err);
     return;
   }
   // The CTA's field is chosen once: the march loop is instantiated per field

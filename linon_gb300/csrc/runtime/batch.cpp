@@ -1,13 +1,15 @@
-// batch.cpp — batched rendering of many views in one persistent launch.
+// batch.cpp — batched rendering of many views in one launch.
 //
 // The reference renders one view per dispatch (MainView::render,
 // src/main_view.rs:831-849) and re-renders at h = 0.001 for Enhance
 // (src/main_view.rs:778-802).  Here any number of views (different size,
-// camera, step size and field) go into one persistent kernel fed by a device
-// work queue; the launch (queue reset + kernel) is captured in a CUDA graph
-// and replayed while the batch shape stays the same.  An autotuner sweeps
-// quantum x block size x tile shape on the caller's batch and caches the
-// winner in the context.
+// camera, step size and field) go into one launch: one CTA per tile of every
+// view, or a persistent kernel fed by a device work queue (warps take whole
+// 32-ray tiles, or refill finished lanes mid-ray); the launch (queue reset +
+// kernel) is captured in a CUDA graph and replayed while the batch shape
+// stays the same.  An autotuner sweeps schedule x block size x tile shape
+// (x quantum for lane refills) on the caller's batch and caches the winner
+// in the context.
 #include <algorithm>
 #include <cstdlib>
 #include <chrono>
@@ -71,6 +73,12 @@ std::string batch_module_source(const std::vector<const linon_field*>& fields) {
        "  linon::march_batch_kernel<1>(LinonFields(), a);\n}\n"
        "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_batch_fk(linon::BatchArgs a) {\n"
        "  linon::march_batch_kernel<2>(LinonFields(), a);\n}\n"
+       "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_queue(linon::BatchArgs a) {\n"
+       "  linon::march_queue_kernel<0>(LinonFields(), a);\n}\n"
+       "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_queue_f(linon::BatchArgs a) {\n"
+       "  linon::march_queue_kernel<1>(LinonFields(), a);\n}\n"
+       "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_queue_fk(linon::BatchArgs a) {\n"
+       "  linon::march_queue_kernel<2>(LinonFields(), a);\n}\n"
        "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_multi(linon::BatchArgs a) {\n"
        "  linon::march_multi_kernel<0>(LinonFields(), a);\n}\n"
        "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_multi_f(linon::BatchArgs a) {\n"
@@ -112,8 +120,8 @@ int get_module(linon_ctx* ctx, BatchState& bs, const linon_field* const* fields,
   std::string log;
   const bool precise = (fv[0]->flags & LINON_COMPILE_PRECISE) != 0;
   int st = jit_compile(batch_module_source(fv), precise,
-                       {"linon_batch", "linon_batch_f", "linon_batch_fk", "linon_multi", "linon_multi_f",
-                        "linon_multi_fk"},
+                       {"linon_batch", "linon_batch_f", "linon_batch_fk", "linon_queue", "linon_queue_f",
+                        "linon_queue_fk", "linon_multi", "linon_multi_f", "linon_multi_fk"},
                        mod, log);
   if (st != LINON_OK) return set_error(st, st == LINON_ECOMPILE ? log : std::string(linon_last_error()));
   bs.modules[key] = mod;
@@ -179,8 +187,8 @@ std::string batched_module_source(const std::vector<const linon_field*>& fields)
 }
 
 // Fields with var<private> state need one field functor per ray for the
-// whole march: the one-CTA-per-tile schedule has it, the persistent queue
-// (a functor per quantum, or per evaluation in a mixed warp) does not.
+// whole march: one CTA per tile and the queue of whole-warp tiles have it,
+// the lane-refilling queue (a functor per quantum) does not.
 bool any_stateful(const linon_field* const* fields, int n_fields) {
   for (int i = 0; i < n_fields; ++i)
     if (fields[i] && fields[i]->stateful) return true;
@@ -191,14 +199,12 @@ int batch_tuning(const linon_ctx* ctx, const linon_batch_tuning* in, linon_batch
   t = linon_batch_tuning{};
   if (in) t = *in;
   else if (ctx->has_tuned) t = ctx->tuned;
-  // default: refill a warp when all its lanes are done (see the autotuner)
   if (t.quantum <= 0) t.quantum = 1024;
   if (t.schedule < 0 || t.schedule > 2) return set_error(LINON_EINVAL, "schedule must be 0, 1 or 2");
-  // auto: one CTA per tile (64 uneven views: 16.4 ms against 20.1 ms for
-  // the best persistent-queue tuning)
+  // auto: one CTA per tile (64 uneven views: 11.2 ms against 11.5 ms for
+  // the queue of warp tiles and 12.5 ms for lane refills below 8)
   if (t.schedule == 0) t.schedule = 2;
-  // 0: refill only at the end of a quantum (measured best on the 64-view
-  // workload: an early refill costs a queue atomic and a camera set-up)
+  // 0: the queue of whole-warp tiles; > 0: refill lanes mid-ray
   if (t.refill_below < 0) t.refill_below = 0;
   if (t.refill_below > 32) t.refill_below = 32;
   if (t.block_threads <= 0) t.block_threads = 128;
@@ -264,16 +270,21 @@ int batch_module(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fie
   return get_module(ctx, g_batch[ctx], fields, n_fields, mod);
 }
 
-const char* batch_kernel_name(const linon_view* views, int n_views, int schedule) {
-  const bool multi = schedule == 2;
+// schedule 1 with refill_below 0: the queue of whole-warp tiles
+// (linon_queue*); with refill_below > 0: the lane-refilling queue
+// (linon_batch*); schedule 2: one CTA per tile (linon_multi*).
+const char* batch_kernel_name(const linon_view* views, int n_views, const linon_batch_tuning& t) {
+  static const char* names[3][3] = {{"linon_batch", "linon_batch_f", "linon_batch_fk"},
+                                    {"linon_queue", "linon_queue_f", "linon_queue_fk"},
+                                    {"linon_multi", "linon_multi_f", "linon_multi_fk"}};
+  const int form = t.schedule == 2 ? 2 : t.refill_below > 0 ? 0 : 1;
   bool kahan = false, plain = false;
   for (int i = 0; i < n_views; ++i) {
-    if (views[i].params.adaptive) return multi ? "linon_multi" : "linon_batch";
+    if (views[i].params.adaptive) return names[form][0];
     (views[i].params.kahan ? kahan : plain) = true;
   }
-  if (kahan && plain) return multi ? "linon_multi" : "linon_batch";
-  if (multi) return kahan ? "linon_multi_fk" : "linon_multi_f";
-  return kahan ? "linon_batch_fk" : "linon_batch_f";
+  if (kahan && plain) return names[form][0];
+  return names[form][kahan ? 2 : 1];
 }
 
 int batch_launch(linon_ctx* ctx, const std::shared_ptr<JitModule>& mod, const linon_batch_tuning& t,
@@ -345,7 +356,7 @@ int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields, int32_t
     if (int st = get_module(ctx, bs, fields, n_fields, mod)) return st;
     linon_batch_tuning t;
     if (int st = batch_tuning(ctx, tuning, t)) return st;
-    if (any_stateful(fields, n_fields)) t.schedule = 2;
+    if (any_stateful(fields, n_fields)) t.refill_below = 0;  // the queue of warp tiles instead
     std::vector<BatchView> tab;
     int n_blocks = 0;
     const long long begin = batch_table(views, n_views, t, tab, &n_blocks);
@@ -366,7 +377,7 @@ int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields, int32_t
     a.refill_below = t.refill_below;
     a.n_blocks = n_blocks;
     a.err = ctx->d_err;
-    cudaKernel_t k = mod->kernels.at(batch_kernel_name(views, n_views, t.schedule));
+    cudaKernel_t k = mod->kernels.at(batch_kernel_name(views, n_views, t));
     dim3 grid, block;
     if (t.schedule == 2) {
       grid = dim3(unsigned(std::max(n_blocks, 1)));
@@ -430,10 +441,8 @@ int linon_autotune_batch(linon_ctx* ctx, const linon_field* const* fields, int32
                          const linon_view* views, int32_t n_views, linon_batch_tuning* best,
                          double* best_ms) {
   if (int st = validate_batch(ctx, fields, n_fields, views, n_views)) return st;
-  // Since the safe-ball radius comes from the distance grid, a warp that
-  // refills only when all its lanes are done (quantum >= the step budget)
-  // is fastest on the uneven-view workload (q 64: 23.3 ms, q 256: 21.4 ms,
-  // q 1024: 20.2 ms; early refill slower at every quantum).
+  // Persistent queue: whole-warp tiles (refill_below 0; quantum unused),
+  // or lanes refilled once fewer than 8 march, every quantum steps.
   const int quanta[] = {256, 1024, 4096};
   const int blocks[] = {128, 256};
   const int tiles[][2] = {{8, 4}, {4, 8}};
@@ -444,11 +453,12 @@ int linon_autotune_batch(linon_ctx* ctx, const linon_field* const* fields, int32
   double best_t = 1e300;
   linon_batch_tuning bt{};
   const bool stateful = any_stateful(fields, n_fields);
-  for (int q : quanta)
-    for (int b : blocks)
-      for (auto& tl : tiles)
-        for (int rf : refills) {
-        if (stateful) continue;  // persistent queue: not for fields with var<private> state
+  for (int rf : refills)
+    for (int q : quanta)
+      for (int b : blocks)
+        for (auto& tl : tiles) {
+        if (stateful && rf > 0) continue;  // lane refills: not for fields with var<private> state
+        if (rf == 0 && q != quanta[0]) continue;  // the quantum plays no part
         linon_batch_tuning t{};
         t.schedule = 1;
         t.quantum = q;

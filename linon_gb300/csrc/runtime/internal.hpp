@@ -102,7 +102,7 @@ int batch_module(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fie
 // The batched kernel for a set of views: linon_batch_f / linon_batch_fk when
 // no view refines its step adaptively and all (or none) use Kahan sums,
 // otherwise the generic linon_batch.
-const char* batch_kernel_name(const linon_view* views, int n_views, int schedule);
+const char* batch_kernel_name(const linon_view* views, int n_views, const linon_batch_tuning& t);
 int batch_launch(linon_ctx* ctx, const std::shared_ptr<JitModule>& mod, const linon_batch_tuning& t,
                  BatchView* views_dev, int n_views, long long total_rays, int n_blocks,
                  unsigned long long* counter, cudaStream_t stream, const char* kernel);
@@ -115,7 +115,7 @@ struct linon_field {
   std::string body, helpers, cuda;
   int flags = 0;
   int flops_arith = 0, flops_transc = 0;
-  bool stateful = false;  // var<private> state: batches use the one-CTA-per-tile schedule
+  bool stateful = false;  // var<private> state: batches never refill lanes mid-ray
   std::string cuda_pair;  // the field in pair form (two rays per thread), "" if none
   mutable int pair_state = 0;  // pair kernels: 0 not tried, 1 compiled, -1 not available
   std::shared_ptr<linon::JitModule> mod;  // capture, field_eval, base march variant

@@ -217,7 +217,7 @@ int launch_wave(linon_server* s, Slot& sl) {
     LINON_CUDA(cudaMemcpyAsync(sl.views_dev, tab.data(), sizeof(BatchView) * tab.size(), cudaMemcpyHostToDevice,
                                sl.main));
     if (int st = batch_launch(ctx, s->mod, s->tuning, sl.views_dev, int(views.size()), total, n_blocks, sl.counter,
-                              sl.main, batch_kernel_name(views.data(), int(views.size()), s->tuning.schedule)))
+                              sl.main, batch_kernel_name(views.data(), int(views.size()), s->tuning)))
       return st;
     for (size_t i = 0; i < renders.size(); ++i) {
       Request* q = renders[i];
@@ -392,7 +392,7 @@ int linon_serve_start(linon_ctx* ctx, const linon_field* const* fields, int32_t 
     if (s->cfg.slots > 8) s->cfg.slots = 8;
     if (s->cfg.max_wave <= 0) s->cfg.max_wave = 256;
     if (int st = batch_tuning(ctx, &s->cfg.tuning, s->tuning)) return st;
-    if (any_stateful(fields, n_fields)) s->tuning.schedule = 2;
+    if (any_stateful(fields, n_fields)) s->tuning.refill_below = 0;  // the queue of warp tiles instead
     if (int st = batch_module(ctx, fields, n_fields, s->mod)) return st;
     // keep freed pool memory cached (no release to the OS between waves)
     cudaMemPool_t pool;

@@ -448,19 +448,23 @@ def snapshot(planes):
     return [{k: getattr(p, k).cpu().numpy().copy() for k in ("color", "mapping", "hit_id", "steps")} for p in planes]
 
 
+BATCH_FORMS = [(1, 0), (1, 8), (2, 0)]  # (schedule, refill_below)
+
+
 @pytest.mark.parametrize("precise", [True, False])
-@pytest.mark.parametrize("schedule", [1, 2])
-def test_batch_equals_plain(engine, precise, schedule):
-    """Both batched forms (1: persistent queue with mid-ray refills, a small
-    quantum; 2: one CTA per tile of every view) against one plain launch per
-    view."""
+@pytest.mark.parametrize("schedule,refill", BATCH_FORMS)
+def test_batch_equals_plain(engine, precise, schedule, refill):
+    """The three batched forms against one plain launch per view: the
+    persistent queue of whole-warp tiles (schedule 1, refill_below 0), the
+    persistent queue that refills lanes mid-ray (refill_below 8, a quantum of
+    16 steps) and one CTA per tile of every view (schedule 2)."""
     flds, views, planes = batch_setup(engine, precise)
     engine.render_views_plain(flds, views)
     a = snapshot(planes)
     for p in planes:
         for k in ("color", "mapping", "hit_id", "steps"):
             getattr(p, k).zero_()
-    tuning = _abi.BatchTuning(16, 64, 0, 8, 4, 0, schedule)
+    tuning = _abi.BatchTuning(16, 64, 0, 8, 4, refill, schedule)
     engine.render_batch(flds, views, tuning)
     engine.synchronize()
     b = snapshot(planes)
@@ -478,13 +482,13 @@ def test_batch_equals_plain(engine, precise, schedule):
             assert np.percentile(d[same], 99) <= 1e-4
 
 
-@pytest.mark.parametrize("schedule", [1, 2])
-def test_batch_eight_fields_equals_plain(engine, schedule):
+@pytest.mark.parametrize("schedule,refill", BATCH_FORMS)
+def test_batch_eight_fields_equals_plain(engine, schedule, refill):
     """The most fields one batch takes (LINON_MAX_BATCH_FIELDS = 8), one view
     per field plus two more: the per-CTA field choice of the tile schedule
-    (one march loop per field) and the per-ray choice of the persistent
-    queue each pick the right field.  Precise modules, bit-exact against one
-    plain launch per view."""
+    and the per-warp choice of the two persistent queues (one march loop per
+    field in each) pick the right field.  Precise modules, bit-exact against
+    one plain launch per view."""
     xyz, faces, rgb = scene.cornell_with_spheres(seed=2, subdivisions=1)
     engine.upload_scene(xyz, faces, rgb, bvh=True)
     # (no "identity": it returns v, which equals linear's v0 on straight rays)
@@ -509,7 +513,7 @@ def test_batch_eight_fields_equals_plain(engine, schedule):
     for p in planes:
         for k in ("color", "mapping", "hit_id", "steps"):
             getattr(p, k).zero_()
-    engine.render_batch(flds, views, _abi.BatchTuning(16, 64, 0, 8, 4, 0, schedule))
+    engine.render_batch(flds, views, _abi.BatchTuning(16, 64, 0, 8, 4, refill, schedule))
     engine.synchronize()
     for x, y in zip(a, snapshot(planes)):
         for k in x:
@@ -616,8 +620,9 @@ def test_private_state_is_per_ray(engine):
     """var<private> lives for one ray: a field that counts its calls and
     turns back after 40 of them (10 RK4 steps) brings every ray of a
     20-step march back to the eye, in the per-frame kernel and in a batch
-    (which then uses the one-CTA-per-tile schedule), next to a stateless
-    field in the same batch."""
+    next to a stateless field (one CTA per tile, the queue of warp tiles,
+    and a lane-refilling request, which then takes the queue of warp
+    tiles)."""
     helpers = "var<private> calls: u32 = 0u;"
     body = "calls += 1u;\nif (calls > 40u) { return -v0; }\nreturn v0;"
     w = wl.plain_small(40, 30)
@@ -643,7 +648,7 @@ def test_private_state_is_per_ray(engine):
         outs.append(fp)
     engine.render_views_plain(flds, views)
     a = snapshot(outs)
-    for tuning in (None, _abi.BatchTuning(1024, 128, 0, 4, 8, 0, 1)):  # a persistent request is overridden
+    for tuning in (None, _abi.BatchTuning(1024, 128, 0, 4, 8, 0, 1), _abi.BatchTuning(16, 128, 0, 4, 8, 8, 1)):
         for fp in outs:
             fp.mapping.zero_()
         engine.render_batch(flds, views, tuning)
