@@ -545,10 +545,13 @@ def bench_batch(eng, stream, wl, torch, dev, predefined_source, keep=None):
 
     plain_ms = timed(lambda: eng.render_views_plain(flds, views))
     steps_plain = sum(int(p.steps.sum().item()) for p in planes)
-    # the persistent work-queue form on its own (each warp takes whole
-    # 4x8-pixel tiles of 32 rays; 128-thread CTAs)
-    pq = _abi.BatchTuning(1024, 128, 0, 4, 8, 0, 1)
-    persistent_ms = timed(lambda: eng.render_batch(flds, views, pq))
+    # the persistent work-queue forms on their own: resident CTAs take
+    # 8x16-pixel tiles from a device counter (schedule 3), or warps take
+    # 4x8-pixel tiles of 32 rays (schedule 1, 128-thread CTAs)
+    forms = {"cta_tiles": _abi.BatchTuning(0, 0, 0, 0, 0, 0, 3),
+             "warp_tiles": _abi.BatchTuning(1024, 128, 0, 4, 8, 0, 1)}
+    form_ms = {k: timed(lambda t=t: eng.render_batch(flds, views, t)) for k, t in forms.items()}
+    best_form = min(form_ms, key=form_ms.get)
     tuning, tune_ms = eng.autotune_batch(flds, views)
     batch_ms = timed(lambda: eng.render_batch(flds, views, tuning))
     eng.synchronize()
@@ -559,11 +562,15 @@ def bench_batch(eng, stream, wl, torch, dev, predefined_source, keep=None):
     return {"views": len(views), "rays": rays, "ray_steps": steps_batch, "plain_ms": plain_ms,
             "batched_ms": batch_ms, "plain_ray_steps_per_s": steps_plain / (plain_ms * 1e-3),
             "batched_ray_steps_per_s": steps_batch / (batch_ms * 1e-3), "speedup": plain_ms / batch_ms,
-            "persistent_queue": {"ms": persistent_ms, "speedup": plain_ms / persistent_ms,
-                                 "tuning": {"form": "warps take whole tiles", "block_threads": 128,
-                                            "tile": [4, 8], "refill_below": 0}},
-            "tuning": {"schedule": {1: "persistent queue" + (" (lane refills)" if tuning.refill_below else ""),
-                                    2: "one CTA per tile"}.get(tuning.schedule, "auto"),
+            "persistent_queue": {"ms": form_ms[best_form], "speedup": plain_ms / form_ms[best_form],
+                                 "form": best_form,
+                                 "forms": {k: {"ms": v, "speedup": plain_ms / v} for k, v in form_ms.items()},
+                                 "cta_tiles": "schedule 3: 8x16-pixel tiles, 128-thread CTAs",
+                                 "warp_tiles": "schedule 1: 4x8-pixel tiles, 128-thread CTAs, refill_below 0"},
+            "tuning": {"schedule": {1: "persistent queue of warp tiles" + (" (lane refills)" if tuning.refill_below
+                                                                           else ""),
+                                    2: "one CTA per tile", 3: "persistent queue of CTA tiles"}.get(tuning.schedule,
+                                                                                                  "auto"),
                        "quantum": tuning.quantum, "block_threads": tuning.block_threads,
                        "tile": [tuning.tile_w, tuning.tile_h], "refill_below": tuning.refill_below}}
 

@@ -353,15 +353,16 @@ int linon_exponent_quantile(linon_ctx* ctx, const float* exponents,
 int linon_outline_indices(uint16_t* out, size_t cap);
 
 /* ---- batched rendering: many views in one launch -----------------------
- * Views of any size, camera, step size and field go into one launch, in
- * one of two schedules: one CTA per 8x16-pixel tile of every view, views
- * with the largest step budget first, the hardware balancing the CTAs (the
- * default); or a persistent kernel over a device work queue of 32-ray
- * tiles (views with the largest step budget first) whose warps each march
- * a whole tile and take the next (refill_below = 0), or retire finished
- * rays and refill free lanes every `quantum` steps once fewer than
- * refill_below lanes march.  fields[] may hold up to
- * LINON_MAX_BATCH_FIELDS distinct fields; views[i].field_index selects.   */
+ * Views of any size, camera, step size and field go into one launch.  The
+ * views' pixels are cut into tiles, views with the largest step budget
+ * first.  Schedules: one CTA per 8x16-pixel tile of every view, the
+ * hardware balancing the CTAs (2, the default); a persistent kernel whose
+ * CTAs take 8x16-pixel tiles from a device work queue (3); a persistent
+ * kernel whose warps take 32-ray tiles from a device work queue and march
+ * each to the end (1, refill_below = 0) or retire finished rays and refill
+ * free lanes every `quantum` steps once fewer than refill_below lanes march
+ * (1, refill_below > 0).  fields[] may hold up to LINON_MAX_BATCH_FIELDS
+ * distinct fields; views[i].field_index selects.                           */
 #define LINON_MAX_BATCH_FIELDS 8
 typedef struct linon_batch_tuning {
   int32_t quantum;          /* lane refills: RK4 steps between retire/refill
@@ -371,9 +372,11 @@ typedef struct linon_batch_tuning {
   int32_t tile_w, tile_h;   /* pixel tile handed out per queue pop (0=auto) */
   int32_t refill_below;     /* 0: warps take whole tiles; > 0: refill free
                                lanes once fewer than this many march        */
-  int32_t schedule;         /* 0 auto (= 2), 1 persistent queue (the
-                               fields above), 2 one CTA per 8x16-pixel tile
-                               of every view (hardware scheduling)          */
+  int32_t schedule;         /* 0 auto (= 2), 1 persistent queue of warp
+                               tiles (the fields above), 2 one CTA per
+                               8x16-pixel tile of every view (hardware
+                               scheduling), 3 persistent queue of 8x16-pixel
+                               CTA tiles (128-thread CTAs)                  */
 } linon_batch_tuning;
 int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields,
                        int32_t n_fields, const linon_view* views,

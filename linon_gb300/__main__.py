@@ -76,8 +76,8 @@ def cmd_batch(a):
         elif a.schedule == 1:
             eng.render_batch(flds, views, _abi.BatchTuning(a.quantum, a.block_threads, a.ctas_per_sm, a.tile[0], a.tile[1],
                                                            a.refill_below, 1))
-        elif a.schedule == 2:
-            eng.render_batch(flds, views, _abi.BatchTuning(0, 0, 0, 0, 0, 0, 2))
+        elif a.schedule in (2, 3):
+            eng.render_batch(flds, views, _abi.BatchTuning(0, 0, a.ctas_per_sm, 0, 0, 0, a.schedule))
         else:
             eng.render_batch(flds, views)
         e.record(stream)
@@ -132,8 +132,9 @@ def main():
     b.add_argument("--seed", type=int, default=0)
     b.add_argument("--repeat", type=int, default=2)
     b.add_argument("--plain", action="store_true")
-    b.add_argument("--schedule", type=int, default=0, choices=(0, 1, 2),
-                   help="0 the default (one CTA per tile), 1 persistent work queue, 2 one CTA per tile")
+    b.add_argument("--schedule", type=int, default=0, choices=(0, 1, 2, 3),
+                   help="0 the default (one CTA per tile), 1 persistent queue of warp tiles, 2 one CTA per tile, "
+                        "3 persistent queue of CTA tiles")
     b.add_argument("--quantum", type=int, default=1024, help="RK4 steps per quantum (persistent queue)")
     b.add_argument("--refill-below", type=int, default=0,
                    help="persistent queue: refill a warp's free lanes once fewer than this many are marching")

@@ -79,6 +79,12 @@ std::string batch_module_source(const std::vector<const linon_field*>& fields) {
        "  linon::march_queue_kernel<1>(LinonFields(), a);\n}\n"
        "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_queue_fk(linon::BatchArgs a) {\n"
        "  linon::march_queue_kernel<2>(LinonFields(), a);\n}\n"
+       "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_tileq(linon::BatchArgs a) {\n"
+       "  linon::march_tileq_kernel<0>(LinonFields(), a);\n}\n"
+       "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_tileq_f(linon::BatchArgs a) {\n"
+       "  linon::march_tileq_kernel<1>(LinonFields(), a);\n}\n"
+       "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_tileq_fk(linon::BatchArgs a) {\n"
+       "  linon::march_tileq_kernel<2>(LinonFields(), a);\n}\n"
        "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_multi(linon::BatchArgs a) {\n"
        "  linon::march_multi_kernel<0>(LinonFields(), a);\n}\n"
        "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_multi_f(linon::BatchArgs a) {\n"
@@ -121,7 +127,8 @@ int get_module(linon_ctx* ctx, BatchState& bs, const linon_field* const* fields,
   const bool precise = (fv[0]->flags & LINON_COMPILE_PRECISE) != 0;
   int st = jit_compile(batch_module_source(fv), precise,
                        {"linon_batch", "linon_batch_f", "linon_batch_fk", "linon_queue", "linon_queue_f",
-                        "linon_queue_fk", "linon_multi", "linon_multi_f", "linon_multi_fk"},
+                        "linon_queue_fk", "linon_multi", "linon_multi_f", "linon_multi_fk", "linon_tileq",
+                        "linon_tileq_f", "linon_tileq_fk"},
                        mod, log);
   if (st != LINON_OK) return set_error(st, st == LINON_ECOMPILE ? log : std::string(linon_last_error()));
   bs.modules[key] = mod;
@@ -200,7 +207,7 @@ int batch_tuning(const linon_ctx* ctx, const linon_batch_tuning* in, linon_batch
   if (in) t = *in;
   else if (ctx->has_tuned) t = ctx->tuned;
   if (t.quantum <= 0) t.quantum = 1024;
-  if (t.schedule < 0 || t.schedule > 2) return set_error(LINON_EINVAL, "schedule must be 0, 1 or 2");
+  if (t.schedule < 0 || t.schedule > 3) return set_error(LINON_EINVAL, "schedule must be 0, 1, 2 or 3");
   // auto: one CTA per tile (64 uneven views: 11.2 ms against 11.5 ms for
   // the queue of warp tiles and 12.5 ms for lane refills below 8)
   if (t.schedule == 0) t.schedule = 2;
@@ -272,12 +279,14 @@ int batch_module(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fie
 
 // schedule 1 with refill_below 0: the queue of whole-warp tiles
 // (linon_queue*); with refill_below > 0: the lane-refilling queue
-// (linon_batch*); schedule 2: one CTA per tile (linon_multi*).
+// (linon_batch*); schedule 2: one CTA per tile (linon_multi*); schedule 3:
+// the queue of CTA tiles (linon_tileq*).
 const char* batch_kernel_name(const linon_view* views, int n_views, const linon_batch_tuning& t) {
-  static const char* names[3][3] = {{"linon_batch", "linon_batch_f", "linon_batch_fk"},
+  static const char* names[4][3] = {{"linon_batch", "linon_batch_f", "linon_batch_fk"},
                                     {"linon_queue", "linon_queue_f", "linon_queue_fk"},
-                                    {"linon_multi", "linon_multi_f", "linon_multi_fk"}};
-  const int form = t.schedule == 2 ? 2 : t.refill_below > 0 ? 0 : 1;
+                                    {"linon_multi", "linon_multi_f", "linon_multi_fk"},
+                                    {"linon_tileq", "linon_tileq_f", "linon_tileq_fk"}};
+  const int form = t.schedule >= 2 ? t.schedule : t.refill_below > 0 ? 0 : 1;
   bool kahan = false, plain = false;
   for (int i = 0; i < n_views; ++i) {
     if (views[i].params.adaptive) return names[form][0];
@@ -313,16 +322,17 @@ int batch_launch(linon_ctx* ctx, const std::shared_ptr<JitModule>& mod, const li
   }
   int sms = 0;
   LINON_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  const int threads = t.schedule == 3 ? 128 : t.block_threads;
   int per_sm = t.ctas_per_sm;
   if (per_sm <= 0) {
     int occ = 0;
-    LINON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)k, t.block_threads,
+    LINON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)k, threads,
                                                              size_t(a.scene.staged_bytes)));
     per_sm = std::max(1, occ);
   }
   LINON_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream));
   void* args[] = {&a};
-  LINON_CUDA(cudaLaunchKernel((const void*)k, dim3(unsigned(sms * per_sm)), dim3(unsigned(t.block_threads)), args,
+  LINON_CUDA(cudaLaunchKernel((const void*)k, dim3(unsigned(sms * per_sm)), dim3(unsigned(threads)), args,
                               size_t(a.scene.staged_bytes), stream));
   return LINON_OK;
 }
@@ -385,15 +395,16 @@ int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields, int32_t
     } else {
       int sms = 0;
       LINON_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+      const int threads = t.schedule == 3 ? 128 : t.block_threads;  // CTA tiles: 128 threads
       int per_sm = t.ctas_per_sm;
       if (per_sm <= 0) {
         int occ = 0;
-        LINON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)k, t.block_threads,
+        LINON_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)k, threads,
                                                                  size_t(a.scene.staged_bytes)));
         per_sm = std::max(1, occ);
       }
       grid = dim3(unsigned(sms * per_sm));
-      block = dim3(unsigned(t.block_threads));
+      block = dim3(unsigned(threads));
     }
     // graph key: the kernel parameters and the launch shape
     std::vector<char> key(sizeof a + sizeof(k) + 2 * sizeof(unsigned));
@@ -487,10 +498,10 @@ int linon_autotune_batch(linon_ctx* ctx, const linon_field* const* fields, int32
           bt = t;
         }
       }
-  {
-    // the one-CTA-per-tile launch
+  for (int sched : {2, 3}) {
+    // one CTA per tile, and the queue of CTA tiles
     linon_batch_tuning t{};
-    t.schedule = 2;
+    t.schedule = sched;
     int st = linon_render_batch(ctx, fields, n_fields, views, n_views, &t);
     if (!st) {
       cudaEventRecord(e0, ctx->stream);

@@ -109,13 +109,14 @@ def test_lyapunov_1024_fast_vs_fp64(engine, acc):
     assert rep["outline_pixels_above_engine_threshold_in_fp64"] >= rep["outline_pixels_checked"] - 1
 
 
-@pytest.mark.parametrize("schedule", [0, 1])
+@pytest.mark.parametrize("schedule", [0, 1, 3])
 def test_batch_uneven_64_fast_vs_fp64(engine, acc, schedule):
     """The 64 uneven views (Cornell room + four 20,480-triangle icospheres
     behind the BVH, stop at the first hit), rendered by one batched launch
-    (schedule 0: the default, one CTA per tile; 1: the persistent work
-    queue): 200 seeded pixels per view against the oracle, whose candidate
-    grid returns the brute-force loop's hits."""
+    (schedule 0: the default, one CTA per tile; 1: the persistent queue of
+    warp tiles; 3: the persistent queue of CTA tiles): 200 seeded pixels per
+    view against the oracle, whose candidate grid returns the brute-force
+    loop's hits."""
     w = wl.batch_uneven(64, seed=0)
     engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
     flds = [engine.compile_field(predefined_source(fid)) for fid in w.fields]
@@ -128,7 +129,7 @@ def test_batch_uneven_64_fast_vs_fp64(engine, acc, schedule):
         v.out = p.abi()
         views.append(v)
         planes.append(p)
-    tuning = None if schedule == 0 else _abi.BatchTuning(1024, 128, 0, 4, 8, 0, 1)
+    tuning = None if schedule == 0 else _abi.BatchTuning(1024, 128, 0, 4, 8, 0, schedule)
     engine.render_batch(flds, views, tuning)
     engine.synchronize()
     torch.cuda.synchronize()

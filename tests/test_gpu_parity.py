@@ -448,16 +448,17 @@ def snapshot(planes):
     return [{k: getattr(p, k).cpu().numpy().copy() for k in ("color", "mapping", "hit_id", "steps")} for p in planes]
 
 
-BATCH_FORMS = [(1, 0), (1, 8), (2, 0)]  # (schedule, refill_below)
+BATCH_FORMS = [(1, 0), (1, 8), (2, 0), (3, 0)]  # (schedule, refill_below)
 
 
 @pytest.mark.parametrize("precise", [True, False])
 @pytest.mark.parametrize("schedule,refill", BATCH_FORMS)
 def test_batch_equals_plain(engine, precise, schedule, refill):
-    """The three batched forms against one plain launch per view: the
+    """The four batched forms against one plain launch per view: the
     persistent queue of whole-warp tiles (schedule 1, refill_below 0), the
     persistent queue that refills lanes mid-ray (refill_below 8, a quantum of
-    16 steps) and one CTA per tile of every view (schedule 2)."""
+    16 steps), one CTA per tile of every view (schedule 2) and the
+    persistent queue of CTA tiles (schedule 3)."""
     flds, views, planes = batch_setup(engine, precise)
     engine.render_views_plain(flds, views)
     a = snapshot(planes)
@@ -485,9 +486,9 @@ def test_batch_equals_plain(engine, precise, schedule, refill):
 @pytest.mark.parametrize("schedule,refill", BATCH_FORMS)
 def test_batch_eight_fields_equals_plain(engine, schedule, refill):
     """The most fields one batch takes (LINON_MAX_BATCH_FIELDS = 8), one view
-    per field plus two more: the per-CTA field choice of the tile schedule
-    and the per-warp choice of the two persistent queues (one march loop per
-    field in each) pick the right field.  Precise modules, bit-exact against
+    per field plus two more: the per-CTA field choice of the tile schedules
+    and the per-warp choice of the warp queues (one march loop per field in
+    each) pick the right field.  Precise modules, bit-exact against
     one plain launch per view."""
     xyz, faces, rgb = scene.cornell_with_spheres(seed=2, subdivisions=1)
     engine.upload_scene(xyz, faces, rgb, bvh=True)
@@ -543,8 +544,8 @@ def test_batch_graph_replay_and_tuning(engine):
         for k in x:
             np.testing.assert_array_equal(x[k], y[k])
     t, ms = engine.autotune_batch(flds, views)
-    assert ms > 0 and (t.schedule == 2 or (t.schedule == 1 and t.quantum in (256, 1024, 4096)
-                                           and t.refill_below in (0, 8)))
+    assert ms > 0 and (t.schedule in (2, 3) or (t.schedule == 1 and t.quantum in (256, 1024, 4096)
+                                                and t.refill_below in (0, 8)))
     # the tuned launch gives the default one's planes (fast modules: the two
     # batched kernels may contract FMAs differently, so to FP32 tolerance)
     engine.render_batch(flds, views, t)
@@ -621,8 +622,8 @@ def test_private_state_is_per_ray(engine):
     turns back after 40 of them (10 RK4 steps) brings every ray of a
     20-step march back to the eye, in the per-frame kernel and in a batch
     next to a stateless field (one CTA per tile, the queue of warp tiles,
-    and a lane-refilling request, which then takes the queue of warp
-    tiles)."""
+    a lane-refilling request, which then takes the queue of warp tiles, and
+    the queue of CTA tiles)."""
     helpers = "var<private> calls: u32 = 0u;"
     body = "calls += 1u;\nif (calls > 40u) { return -v0; }\nreturn v0;"
     w = wl.plain_small(40, 30)
@@ -648,7 +649,8 @@ def test_private_state_is_per_ray(engine):
         outs.append(fp)
     engine.render_views_plain(flds, views)
     a = snapshot(outs)
-    for tuning in (None, _abi.BatchTuning(1024, 128, 0, 4, 8, 0, 1), _abi.BatchTuning(16, 128, 0, 4, 8, 8, 1)):
+    for tuning in (None, _abi.BatchTuning(1024, 128, 0, 4, 8, 0, 1), _abi.BatchTuning(16, 128, 0, 4, 8, 8, 1),
+                   _abi.BatchTuning(0, 0, 0, 0, 0, 0, 3)):
         for fp in outs:
             fp.mapping.zero_()
         engine.render_batch(flds, views, tuning)
