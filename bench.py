@@ -126,11 +126,11 @@ def flops_per_step(pyoracle, w, fid):
 
 def kernel_name(field, label):
     """The march kernel a 1080p frame of `field` runs: two rays per thread
-    (v30) when the field has a compiled pair form and at least 14 FP32
+    (v30) when the field has a compiled pair form and at least 4 FP32
     operations and at most one transcendental per evaluation (the engine's
     rule; 1080p frames fill the GPU), else one ray per thread (v14)."""
     arith, transc = field.flops()
-    pairs = field.pair_state() == 1 and arith >= 14 and transc <= 1
+    pairs = field.pair_state() == 1 and arith >= 4 and transc <= 1
     return (f"linon_march_v{30 if pairs else 14} ({label} field; fixed steps, Kahan, field_weight 1; "
             f"{'two rays' if pairs else 'one ray'} per thread)")
 

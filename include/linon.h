@@ -232,10 +232,12 @@ const char* linon_field_cuda_source(const linon_field* field);
 /* Whether fixed-step renders of this field can run two rays per thread (no
  * counterpart in the reference, whose shader marches one ray per
  * invocation): 1 the pair kernels compiled (a render uses them when the
- * field's arithmetic dominates the step and the frame is large; the
- * environment variable LINON_RAY_PAIRS=0 / =1 forces one / two rays per
- * thread), 0 the field has a pair form not tried yet, -1 it has none (a
- * branch on a value, a precise module) or it did not compile.             */
+ * field has at least 4 FP32 operations and at most one transcendental per
+ * evaluation and the frame fills at least 8 waves of the pair kernel's
+ * resident CTAs; the environment variable LINON_RAY_PAIRS=0 / =1 forces
+ * one / two rays per thread), 0 the field has a pair form not tried yet,
+ * -1 it has none (a branch on a value, var<private> state, a precise
+ * module) or it did not compile.                                           */
 int linon_field_pair_state(const linon_field* field);
 /* Front end + NVRTC compile for sm_103a without loading (no GPU needed): the
  * naga validation step of create_shader_module (main_view.rs:662-665).  On

@@ -828,7 +828,17 @@ __device__ __forceinline__ void march_pair_kernel(const F& field, const MarchArg
   constexpr bool W1 = (V & V_W1) != 0;
   extern __shared__ float4 linon_smem[];
   __shared__ unsigned long long mbar;
-  const SceneView sc = cta_scene(a.scene, linon_smem, &mbar, a.err);
+  // The scene view lives in shared memory: only the (rare) segment test
+  // reads it, and the march keeps its registers for the two rays (96
+  // registers without spills, 5 CTAs per SM: the 1080p lens frame 28.02 ->
+  // 27.63 ms against the view in registers, 80 registers with spills).
+  __shared__ SceneView scene_sh;
+  {
+    const SceneView v = cta_scene(a.scene, linon_smem, &mbar, a.err);
+    if (threadIdx.x == 0) scene_sh = v;
+    __syncthreads();
+  }
+  const SceneView& sc = scene_sh;
   const int W = a.frame.W, H = a.frame.H;
   const int pairs_w = a.tile_w / 2;
   const int lx = threadIdx.x % pairs_w, ly = threadIdx.x / pairs_w;

@@ -738,22 +738,23 @@ int launch_rows(linon_ctx* ctx, const linon_field* field, const linon_camera* ca
   // adaptive retries, early stop or linear mode, when the field has a pair
   // form that compiles (the first such render compiles it).  Pairs halve
   // the FP32 issue of the field and the step but leave the FMA pipe's work
-  // as it is and hold more registers (fewer warps per SM, CTAs with twice
-  // the work), so they pay only where the field's arithmetic dominates the
-  // step and the frame fills the GPU many times over: measured at 1080p x
-  // 4000 steps, lens (24 operations and one transcendental per evaluation)
-  // 29.2 -> 28.1 ms and the scaled Lorenz field (14, 0) 21.1 -> 20.3 ms, but
-  // twist (16 and a sine and cosine) 19.5 -> 21.0 ms, linear (0) 6.3 -> 8.7
-  // ms, and the Lorenz field at 1024^2 (4.5 waves of pair CTAs) 7.4 -> 8.5
-  // ms.  Rule: at least 14 FP32 operations and at most one transcendental
-  // per evaluation, and a frame of at least 8 waves of the pair kernel's
-  // resident CTAs.
+  // as it is, run sines and cosines lane by lane, and hold more registers
+  // (fewer warps per SM, CTAs with twice the work).  Measured at 1080p x
+  // 4000 steps (ms, one ray / two rays per thread; FP32 operations and
+  // transcendentals per evaluation): translation_x (4, 0) 11.76 / 10.87,
+  // roessler (6, 0) 15.47 / 14.29, lorenz (8, 0) 19.72 / 18.58, scaled
+  // Lorenz (14, 0) 21.10 / 20.13, lens (24, 1) 29.25 / 27.63; but linear
+  // (0, 0) 6.34 / 8.02, twist (16, 2) 19.58 / 21.84, rotation (28, 2)
+  // 26.52 / 27.13, and the scaled Lorenz field at 1024^2 x 2000 (under 8
+  // waves of pair CTAs) 7.05 / 8.34.  Rule: at least 4 FP32 operations and
+  // at most one transcendental per evaluation, and a frame of at least 8
+  // waves of the pair kernel's resident CTAs.
   // LINON_RAY_PAIRS=0 / =1 forces one ray / two rays per thread.
   const char* force = std::getenv("LINON_RAY_PAIRS");
   bool pairs = !precise && (v & 4) && !(v & 1) && !params->stop_on_hit && !params->linear_mode &&
                !field->cuda_pair.empty() && field->pair_state >= 0 && !(force && force[0] == '0');
   if (pairs && !(force && force[0] == '1'))
-    pairs = field->flops_arith >= 14 && field->flops_transc <= 1;
+    pairs = field->flops_arith >= 4 && field->flops_transc <= 1;
   if (pairs) {
     if (march_kernel(field, v | 16, &k) == LINON_OK) {
       field->pair_state = 1;
