@@ -927,7 +927,7 @@ int linon_ftle(linon_ctx* ctx, const linon_camera* camera, const linon_march_par
   a.H = height;
   a.focal_length = params->focal_length;
   a.viewport_height = params->viewport_height;
-  a.T = double(horizon_T);
+  a.half_over_T = 0.5 / double(horizon_T);
   LINON_CUDA(launch_ftle(a, ctx->stream));
   return LINON_OK;
   LINON_TRY_END

@@ -186,7 +186,7 @@ __global__ void ftle_kernel(FtleArgs a) {
       best_dd = dd;
     }
   }
-  a.out[ci] = best_de > 0.0 ? float(0.5 * log(best_de / best_dd) / a.T) : -__int_as_float(0x7f800000);
+  a.out[ci] = best_de > 0.0 ? float(log(best_de / best_dd) * a.half_over_T) : -__int_as_float(0x7f800000);
 }
 
 // Outline selection.  Each of the shader's 8 scans picks either the last

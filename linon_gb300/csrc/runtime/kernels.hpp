@@ -25,7 +25,7 @@ struct FtleArgs {
   float* out;
   int W, H;
   float focal_length, viewport_height;
-  double T;
+  double half_over_T;  // 0.5 / T, in FP64 (a multiply per pixel instead of a divide)
 };
 
 cudaError_t launch_overlay(const OverlayArgs& a, bool fp64, cudaStream_t s);
