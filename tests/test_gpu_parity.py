@@ -484,6 +484,43 @@ def test_batch_equals_plain(engine, precise, schedule, refill):
 
 
 @pytest.mark.parametrize("schedule,refill", BATCH_FORMS)
+def test_batch_tiny_and_mixed_views_equal_plain(engine, schedule, refill):
+    """Views smaller than one tile or one warp (1x1, 1x37, 33x1, 7x5), one
+    just past a tile edge (17x16), and mixed march parameters in one batch:
+    fixed steps with Kahan sums and stop at the first hit, a single step,
+    linear mode, the shader's own adaptive t-loop.  Precise modules, every
+    batched form bit-exact against one plain launch per view."""
+    xyz, faces, rgb = scene.cornell_with_spheres(seed=5, subdivisions=1)
+    engine.upload_scene(xyz, faces, rgb, bvh=True)
+    flds = [field(engine, nme, True) for nme in ("linear", "twist", "lorenz_scaled")]
+    cams = wl.batch_views(7, seed=21, min_side=20, max_side=40, n_fields=3)
+    sizes = [(1, 1), (1, 37), (33, 1), (7, 5), (17, 16), (40, 3), (9, 9)]
+    plist = [wl.fixed_steps(0.02, 150, kahan=True, stop_on_hit=True), wl.fixed_steps(0.05, 1, kahan=True),
+             wl.fixed_steps(0.02, 120, kahan=False), _abi.shader_params(), wl.fixed_steps(0.01, 90, kahan=True),
+             wl.fixed_steps(0.02, 60, kahan=True, stop_on_hit=True), wl.fixed_steps(0.02, 80, kahan=True)]
+    plist[2].linear_mode = 1
+    views, planes = [], []
+    for i, ((W, H), (_w, _h, camera, _p, fidx), params) in enumerate(zip(sizes, cams, plist)):
+        fp = FramePlanes.allocate(W, H)
+        v = _abi.View()
+        v.camera, v.settings, v.params = camera, wl.settings(), params
+        v.width, v.height, v.field_index = W, H, i % 3
+        v.out = fp.abi()
+        views.append(v)
+        planes.append(fp)
+    engine.render_views_plain(flds, views)
+    a = snapshot(planes)
+    for p in planes:
+        for k in ("color", "mapping", "hit_id", "steps"):
+            getattr(p, k).fill_(7)
+    engine.render_batch(flds, views, _abi.BatchTuning(16, 64, 0, 8, 4, refill, schedule))
+    engine.synchronize()
+    for i, (x, y) in enumerate(zip(a, snapshot(planes))):
+        for k in x:
+            np.testing.assert_array_equal(x[k], y[k], err_msg=f"view {i} {sizes[i]} {k}")
+
+
+@pytest.mark.parametrize("schedule,refill", BATCH_FORMS)
 def test_batch_eight_fields_equals_plain(engine, schedule, refill):
     """The most fields one batch takes (LINON_MAX_BATCH_FIELDS = 8), one view
     per field plus two more: the per-CTA field choice of the tile schedules
