@@ -1243,23 +1243,26 @@ __device__ __forceinline__ void march_multi_kernel(const Fields& fields, const B
   march_tile_block<MODE>(fields, a, sc, int(blockIdx.x));
 }
 
-// Persistent queue of CTA tiles: one CTA per resident slot takes the next
-// 8 x 16-pixel tile (the one-CTA-per-tile schedule's tiles and order) from a
-// device counter, marches it and takes the next, until the counter passes
-// the last tile.
+// Persistent queue of CTA tiles: one CTA per resident slot marches the
+// 8 x 16-pixel tile of its own index first (the one-CTA-per-tile schedule's
+// tiles and order), then takes the next tile from a device counter (which
+// starts past the grid's first tiles), until the counter passes the last
+// tile.  Thread 0 takes the next tile when its own rays of the current one
+// are done; two slots for the taken index leave one barrier per tile.
 template <int MODE = 0, class Fields>
 __device__ __forceinline__ void march_tileq_kernel(const Fields& fields, const BatchArgs& a) {
   extern __shared__ float4 linon_smem[];
   __shared__ unsigned long long mbar;
-  __shared__ int next_tile;
+  __shared__ int next_tile[2];
   const SceneView sc = cta_scene(a.scene, linon_smem, &mbar, a.err);
-  for (;;) {
-    if (threadIdx.x == 0) next_tile = int(atomicAdd(a.counter, 1ull));
-    __syncthreads();
-    const int block = next_tile;
-    __syncthreads();  // every thread has read next_tile before it is overwritten
-    if (block >= a.n_blocks) break;
+  int block = int(blockIdx.x), slot = 0;
+  while (block < a.n_blocks) {
     march_tile_block<MODE>(fields, a, sc, block);
+    if (threadIdx.x == 0) next_tile[slot] = int(gridDim.x + atomicAdd(a.counter, 1ull));
+    // the slot written here was last read before the previous barrier
+    __syncthreads();
+    block = next_tile[slot];
+    slot ^= 1;
   }
 }
 
