@@ -34,7 +34,57 @@ struct BatchState {
 std::mutex g_bmu;
 std::map<const linon_ctx*, BatchState> g_batch;
 
-std::string batch_module_source(const std::vector<const linon_field*>& fields) {
+// The batched kernels: entry name, launch bounds, kernel template, mode
+// (0 any views, 1 fixed steps, 2 fixed steps with Kahan sums).  A module
+// holds the entries one launch form needs, so a first launch compiles three
+// march loops per field instead of twelve.
+struct BatchEntry {
+  const char* name;
+  const char* bounds;
+  const char* body;
+  int mode;
+};
+const BatchEntry kBatchEntries[] = {
+    {"linon_batch", "LINON_BATCH_BOUNDS", "march_batch_kernel", 0},
+    {"linon_batch_f", "LINON_BATCH_BOUNDS", "march_batch_kernel", 1},
+    {"linon_batch_fk", "LINON_BATCH_BOUNDS", "march_batch_kernel", 2},
+    {"linon_queue", "LINON_BATCH_BOUNDS", "march_queue_kernel", 0},
+    {"linon_queue_f", "LINON_BATCH_BOUNDS", "march_queue_kernel", 1},
+    {"linon_queue_fk", "LINON_BATCH_BOUNDS", "march_queue_kernel", 2},
+    {"linon_multi", "LINON_MULTI_BOUNDS", "march_multi_kernel", 0},
+    {"linon_multi_f", "LINON_MULTI_BOUNDS", "march_multi_kernel", 1},
+    {"linon_multi_fk", "LINON_MULTI_BOUNDS", "march_multi_kernel", 2},
+    {"linon_tileq", "LINON_MULTI_BOUNDS", "march_tileq_kernel", 0},
+    {"linon_tileq_f", "LINON_MULTI_BOUNDS", "march_tileq_kernel", 1},
+    {"linon_tileq_fk", "LINON_MULTI_BOUNDS", "march_tileq_kernel", 2},
+};
+
+const BatchEntry* batch_entry(const std::string& name) {
+  for (const BatchEntry& e : kBatchEntries)
+    if (name == e.name) return &e;
+  return nullptr;
+}
+
+// The three modes of one launch form (the form of `kernel`).
+std::vector<std::string> form_kernels(const std::string& kernel) {
+  std::string base = kernel;
+  for (const char* suffix : {"_fk", "_f"})
+    if (base.size() > std::strlen(suffix) && base.compare(base.size() - std::strlen(suffix), std::string::npos,
+                                                          suffix) == 0) {
+      base.resize(base.size() - std::strlen(suffix));
+      break;
+    }
+  return {base, base + "_f", base + "_fk"};
+}
+
+std::vector<std::string> all_batch_kernels() {
+  std::vector<std::string> k;
+  for (const BatchEntry& e : kBatchEntries) k.push_back(e.name);
+  return k;
+}
+
+std::string batch_module_source(const std::vector<const linon_field*>& fields,
+                                const std::vector<std::string>& kernels) {
   std::ostringstream s;
   s << "#include \"march.cuh\"\n";
   for (size_t i = 0; i < fields.size(); ++i) {
@@ -66,31 +116,13 @@ std::string batch_module_source(const std::vector<const linon_field*>& fields) {
        "    switch (i) {\n";
   for (size_t i = 1; i < fields.size(); ++i) s << "      case " << i << ": fn(LinonField" << i << "()); return;\n";
   s << "      default: fn(LinonField0()); return;\n"
-       "    }\n  }\n};\n"
-       "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_batch(linon::BatchArgs a) {\n"
-       "  linon::march_batch_kernel<0>(LinonFields(), a);\n}\n"
-       "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_batch_f(linon::BatchArgs a) {\n"
-       "  linon::march_batch_kernel<1>(LinonFields(), a);\n}\n"
-       "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_batch_fk(linon::BatchArgs a) {\n"
-       "  linon::march_batch_kernel<2>(LinonFields(), a);\n}\n"
-       "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_queue(linon::BatchArgs a) {\n"
-       "  linon::march_queue_kernel<0>(LinonFields(), a);\n}\n"
-       "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_queue_f(linon::BatchArgs a) {\n"
-       "  linon::march_queue_kernel<1>(LinonFields(), a);\n}\n"
-       "extern \"C\" __global__ void LINON_BATCH_BOUNDS linon_queue_fk(linon::BatchArgs a) {\n"
-       "  linon::march_queue_kernel<2>(LinonFields(), a);\n}\n"
-       "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_tileq(linon::BatchArgs a) {\n"
-       "  linon::march_tileq_kernel<0>(LinonFields(), a);\n}\n"
-       "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_tileq_f(linon::BatchArgs a) {\n"
-       "  linon::march_tileq_kernel<1>(LinonFields(), a);\n}\n"
-       "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_tileq_fk(linon::BatchArgs a) {\n"
-       "  linon::march_tileq_kernel<2>(LinonFields(), a);\n}\n"
-       "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_multi(linon::BatchArgs a) {\n"
-       "  linon::march_multi_kernel<0>(LinonFields(), a);\n}\n"
-       "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_multi_f(linon::BatchArgs a) {\n"
-       "  linon::march_multi_kernel<1>(LinonFields(), a);\n}\n"
-       "extern \"C\" __global__ void LINON_MULTI_BOUNDS linon_multi_fk(linon::BatchArgs a) {\n"
-       "  linon::march_multi_kernel<2>(LinonFields(), a);\n}\n";
+       "    }\n  }\n};\n";
+  for (const std::string& k : kernels) {
+    const BatchEntry* e = batch_entry(k);
+    if (!e) continue;
+    s << "extern \"C\" __global__ void " << e->bounds << " " << e->name << "(linon::BatchArgs a) {\n  linon::"
+      << e->body << "<" << e->mode << ">(LinonFields(), a);\n}\n";
+  }
   return s.str();
 }
 
@@ -112,10 +144,11 @@ int dev_grow(linon_ctx* ctx, DevBuf& b, size_t bytes) {
 }
 
 int get_module(linon_ctx* ctx, BatchState& bs, const linon_field* const* fields, int32_t n_fields,
-               std::shared_ptr<JitModule>& mod) {
+               const std::vector<std::string>& kernels, std::shared_ptr<JitModule>& mod) {
   std::vector<const linon_field*> fv(fields, fields + n_fields);
   std::string key;
   for (auto* f : fv) key += f->cuda + "\x01" + std::to_string(f->flags) + "\x02";
+  for (auto& k : kernels) key += k + "\x03";
   // the extra compiler options are part of what the module is
   if (const char* extra = std::getenv("LINON_JIT_OPTIONS")) key += extra;
   auto it = bs.modules.find(key);
@@ -125,11 +158,7 @@ int get_module(linon_ctx* ctx, BatchState& bs, const linon_field* const* fields,
   }
   std::string log;
   const bool precise = (fv[0]->flags & LINON_COMPILE_PRECISE) != 0;
-  int st = jit_compile(batch_module_source(fv), precise,
-                       {"linon_batch", "linon_batch_f", "linon_batch_fk", "linon_queue", "linon_queue_f",
-                        "linon_queue_fk", "linon_multi", "linon_multi_f", "linon_multi_fk", "linon_tileq",
-                        "linon_tileq_f", "linon_tileq_fk"},
-                       mod, log);
+  int st = jit_compile(batch_module_source(fv, kernels), precise, kernels, mod, log);
   if (st != LINON_OK) return set_error(st, st == LINON_ECOMPILE ? log : std::string(linon_last_error()));
   bs.modules[key] = mod;
   (void)ctx;
@@ -190,7 +219,7 @@ int validate_batch(const linon_ctx* ctx, const linon_field* const* fields, int32
 // The batched module (persistent and one-CTA-per-tile kernels) for a list of
 // fields, for compile checks without a context.
 std::string batched_module_source(const std::vector<const linon_field*>& fields) {
-  return batch_module_source(fields);
+  return batch_module_source(fields, all_batch_kernels());
 }
 
 // Fields with var<private> state need one field functor per ray for the
@@ -271,10 +300,13 @@ long long batch_table(const linon_view* views, int n_views, const linon_batch_tu
   return begin;
 }
 
-int batch_module(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fields,
+int batch_module(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fields, const linon_batch_tuning& t,
                  std::shared_ptr<JitModule>& mod) {
+  // the three modes of the tuning's launch form (a wave's views decide which)
+  linon_view v{};
+  v.params.kahan = 1;
   std::lock_guard<std::mutex> lock(g_bmu);
-  return get_module(ctx, g_batch[ctx], fields, n_fields, mod);
+  return get_module(ctx, g_batch[ctx], fields, n_fields, form_kernels(batch_kernel_name(&v, 1, t)), mod);
 }
 
 // schedule 1 with refill_below 0: the queue of whole-warp tiles
@@ -362,11 +394,12 @@ int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields, int32_t
     LINON_CUDA(cudaSetDevice(ctx->device));
     std::lock_guard<std::mutex> lock(g_bmu);
     BatchState& bs = g_batch[ctx];
-    std::shared_ptr<JitModule> mod;
-    if (int st = get_module(ctx, bs, fields, n_fields, mod)) return st;
     linon_batch_tuning t;
     if (int st = batch_tuning(ctx, tuning, t)) return st;
     if (any_stateful(fields, n_fields)) t.refill_below = 0;  // the queue of warp tiles instead
+    const char* kname = batch_kernel_name(views, n_views, t);
+    std::shared_ptr<JitModule> mod;
+    if (int st = get_module(ctx, bs, fields, n_fields, {kname}, mod)) return st;
     std::vector<BatchView> tab;
     int n_blocks = 0;
     const long long begin = batch_table(views, n_views, t, tab, &n_blocks);
@@ -387,7 +420,7 @@ int linon_render_batch(linon_ctx* ctx, const linon_field* const* fields, int32_t
     a.refill_below = t.refill_below;
     a.n_blocks = n_blocks;
     a.err = ctx->d_err;
-    cudaKernel_t k = mod->kernels.at(batch_kernel_name(views, n_views, t));
+    cudaKernel_t k = mod->kernels.at(kname);
     dim3 grid, block;
     if (t.schedule == 2) {
       grid = dim3(unsigned(std::max(n_blocks, 1)));

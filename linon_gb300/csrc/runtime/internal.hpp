@@ -97,7 +97,8 @@ void batch_release(linon_ctx* ctx);
 int batch_tuning(const linon_ctx* ctx, const linon_batch_tuning* in, linon_batch_tuning& t);
 long long batch_table(const linon_view* views, int n_views, const linon_batch_tuning& t,
                       std::vector<BatchView>& tab, int* n_blocks = nullptr);
-int batch_module(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fields,
+// The module of the tuning's launch form (its three step modes).
+int batch_module(linon_ctx* ctx, const linon_field* const* fields, int32_t n_fields, const linon_batch_tuning& t,
                  std::shared_ptr<JitModule>& mod);
 // The batched kernel for a set of views: linon_batch_f / linon_batch_fk when
 // no view refines its step adaptively and all (or none) use Kahan sums,

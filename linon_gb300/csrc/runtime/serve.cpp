@@ -393,7 +393,7 @@ int linon_serve_start(linon_ctx* ctx, const linon_field* const* fields, int32_t 
     if (s->cfg.max_wave <= 0) s->cfg.max_wave = 256;
     if (int st = batch_tuning(ctx, &s->cfg.tuning, s->tuning)) return st;
     if (any_stateful(fields, n_fields)) s->tuning.refill_below = 0;  // the queue of warp tiles instead
-    if (int st = batch_module(ctx, fields, n_fields, s->mod)) return st;
+    if (int st = batch_module(ctx, fields, n_fields, s->tuning, s->mod)) return st;
     // keep freed pool memory cached (no release to the OS between waves)
     cudaMemPool_t pool;
     LINON_CUDA(cudaDeviceGetDefaultMemPool(&pool, ctx->device));
