@@ -1277,6 +1277,7 @@ __device__ __forceinline__ void capture_kernel(const F& field, const CaptureArgs
   float t = 0.0f;
   const float h = a.h, hh = 0.5f * a.h, w = a.field_weight;
   float4* out = a.out + size_t(ray) * a.n_points;
+  int until = 0, slot = 0;  // steps before the next recorded point (every `every` steps from 0), its slot
   for (int i = 0; i < a.n_steps; ++i) {
     const vec3f k1 = field(p, p, start_dir, dir, t);
     const vec3f k2 = field(p, p + hh * k1, start_dir, k1, t + hh);
@@ -1285,7 +1286,11 @@ __device__ __forceinline__ void capture_kernel(const F& field, const CaptureArgs
     const vec3f v = rk4_combine(k1, k2, k3, k4);
     dir = wgsl::vmadd(v, w, (1.0f - w) * dir);
     const vec3f step_dir = wgsl::vscale(dir, h);
-    if (i % a.every == 0) out[i / a.every] = make_float4(p.x, p.y, p.z, 1.0f);
+    if (until == 0) {
+      out[slot++] = make_float4(p.x, p.y, p.z, 1.0f);
+      until = a.every;
+    }
+    --until;
     p = wgsl::vadd(p, step_dir);
     t = t + h;
   }
