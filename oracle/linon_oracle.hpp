@@ -834,6 +834,8 @@ inline RayResult<T> render_pixel(const Scene& sc, int field, const CameraBasis<T
 
 // sample_rays, main_view.wgsl:281-314: records the position before every
 // `every`-th step; n_steps steps of size h, no intersection, no adaptivity.
+// With record_final the final position follows the recorded ones (slot
+// ceil(n_steps / every), the general capture's layout).
 template <class T>
 inline void sample_ray(int field, V3<T> start_point, V3<T> start_dir, T field_weight, T h,
                        int n_steps, int every, bool record_final, float* out /* npts*4 */) {
@@ -855,8 +857,8 @@ inline void sample_ray(int field, V3<T> start_point, V3<T> start_dir, T field_we
     cur_point = cur_point + step_dir;
     t = t + h;
   }
-  if (record_final) {
-    float* o = out + 4 * (n_steps / every);
+  if (record_final) {  // after the ceil(n_steps / every) recorded points
+    float* o = out + 4 * ((n_steps + every - 1) / every);
     o[0] = float(cur_point.x); o[1] = float(cur_point.y); o[2] = float(cur_point.z); o[3] = 1.0f;
   }
 }

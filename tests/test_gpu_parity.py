@@ -386,12 +386,16 @@ def test_capture_reference_matches_oracle(engine, oracle):
     np.testing.assert_array_equal(got[1, 0, 4:7], [0.5, 0.5, 0.0])
 
 
-def test_capture_paths_matches_oracle(engine, oracle):
+@pytest.mark.parametrize("n_steps,every", [(301, 7), (300, 1), (5, 10), (0, 3), (49, 49), (50, 49)])
+def test_capture_paths_matches_oracle(engine, oracle, n_steps, every):
+    """Recorded points every `every` steps from step 0, plus the final
+    point: a step count that `every` does not divide, every step, fewer
+    steps than `every`, no step, and `every` equal to the step count or one
+    below it; bit-exact with the oracle (precise module)."""
     w = wl.plain_small(64, 64)
     fld = field(engine, "translation_x", True)
     rng = np.random.default_rng(3)
     pos = rng.uniform(0.2, 0.8, size=(37, 2)).astype(np.float32)
-    n_steps, every = 301, 7
     npts = -(-n_steps // every) + 1
     out = torch.zeros((37, npts, 4), dtype=torch.float32, device="cuda")
     engine.capture_paths(fld, w.camera, w.settings, w.params, 64, 64, pos, 0.01, n_steps, every, out)
