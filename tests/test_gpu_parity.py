@@ -356,6 +356,31 @@ def test_overlay_matches_oracle(engine, oracle, fp64, srgb):
     assert np.abs(target.cpu().numpy().astype(int) - o_rgba.astype(int)).max() <= 1
 
 
+@pytest.mark.parametrize("delta", [1, 9, 10, 30])
+def test_overlay_border_widths_match_oracle(engine, oracle, delta):
+    """A non-square frame (96x40) with central-difference deltas whose 2*delta
+    border leaves a few interior rows (9), none (10: rows 20..19) or covers
+    the frame (30); both overlay modes; the exponents buffer is pre-filled
+    with a sentinel, which border pixels keep in the engine as in the
+    oracle."""
+    w = wl.lyapunov_1024(96, 40)
+    w.params = wl.fixed_steps(0.01, 150, kahan=True)
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    g = gpu_render(engine, w, field(engine, "lorenz_scaled", False))
+    color = torch.from_numpy(g["color"]).cuda()
+    mapping = torch.from_numpy(g["mapping"]).cuda()
+    for mode in (0, 1):
+        st = wl.settings(overlay_mode=mode, delta=delta, scaling=50.0)
+        target = torch.empty((40, 96, 4), dtype=torch.uint8, device="cuda")
+        expo = torch.full((40, 96), -7.0, dtype=torch.float32, device="cuda")
+        engine.overlay(st, 96, 40, color, mapping, target, expo, srgb=False, fp64=True)
+        torch.cuda.synchronize()
+        o_e = np.full((40, 96), -7.0, np.float32)
+        o_rgba, o_e = oracle.overlay(g["color"], g["mapping"], 96, 40, st, srgb=False, precision=64, exponents=o_e)
+        np.testing.assert_allclose(expo.cpu().numpy(), o_e, rtol=1e-5, atol=1e-6)
+        assert np.abs(target.cpu().numpy().astype(int) - o_rgba.astype(int)).max() <= 1
+
+
 def test_ftle_matches_oracle(engine, oracle):
     w = wl.lyapunov_1024(96, 96)
     w.params = wl.fixed_steps(0.01, 200, kahan=True)
