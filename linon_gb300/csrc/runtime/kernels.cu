@@ -235,8 +235,10 @@ __global__ void outline_init_kernel(unsigned long long* slots) {
   if (g == 8) slots[8] = 0ull;
 }
 
-// Order-preserving key of a float (NaN sorts last).
+// Order-preserving key of a float; every NaN, whatever its sign bit, sorts
+// last (as numpy's sort puts them), with the key of a NaN.
 __device__ __forceinline__ unsigned fkey(float f) {
+  if (f != f) return 0xffffffffu;
   unsigned u = __float_as_uint(f);
   return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }

@@ -452,6 +452,47 @@ def test_quantile_matches_numpy(engine):
         assert got == inner[int(np.floor(q * (len(inner) - 1)))]
 
 
+def test_quantile_with_infinities_nans_and_signed_zeros(engine):
+    """Exponent maps hold -inf (isolated pixels of the finite-time
+    exponent), +inf and NaN of either sign; the quantile is numpy's sorted
+    value at floor(q (n - 1)) with every NaN last and -0.0 equal to +0.0."""
+    rng = np.random.default_rng(11)
+    e = rng.standard_normal((60, 70)).astype(np.float32)
+    flat = e.reshape(-1)
+    idx = rng.permutation(flat.size)
+    flat[idx[:40]] = -np.inf
+    flat[idx[40:60]] = np.inf
+    flat[idx[60:80]] = np.nan
+    flat[idx[80:100]] = -np.float32(np.nan)
+    flat[idx[100:130]] = 0.0
+    flat[idx[130:160]] = -0.0
+    assert np.signbit(flat[idx[80:100]]).all()
+    t = torch.from_numpy(e).cuda()
+    for border in (0, 2):
+        inner = np.sort(e[border:60 - border, border:70 - border].ravel())
+        for q in (0.0, 0.004, 0.25, 0.5, 0.9, 0.97, 0.99, 1.0):
+            got = engine.exponent_quantile(t, 70, 60, q, border=border)
+            want = inner[int(np.floor(q * (len(inner) - 1)))]
+            assert (np.isnan(got) and np.isnan(want)) or got == want, (border, q, got, want)
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (2, 1), (1, 3), (5, 4)])
+def test_ftle_tiny_frames_match_oracle(engine, oracle, shape):
+    """Frames of one pixel (no neighbour: -inf; its ray direction is NaN as in
+    the shader) and frames one pixel wide or high."""
+    W, H = shape
+    w = wl.lyapunov_1024(W, H)
+    w.params = wl.fixed_steps(0.01, 50, kahan=True)
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    g = gpu_render(engine, w, field(engine, "lorenz_scaled", False))
+    mapping = torch.from_numpy(g["mapping"]).cuda()
+    out = torch.empty((H, W), dtype=torch.float32, device="cuda")
+    engine.ftle(w.camera, w.params, W, H, mapping, 0.5, out)
+    torch.cuda.synchronize()
+    o = oracle.ftle(w.camera, w.params, W, H, g["mapping"], 0.5)
+    np.testing.assert_allclose(out.cpu().numpy(), o, rtol=1e-6, atol=1e-6)
+
+
 def batch_setup(engine, precise, n=6, seed=4):
     xyz, faces, rgb = scene.cornell_with_spheres(seed=seed, subdivisions=2)
     engine.upload_scene(xyz, faces, rgb, bvh=True)
