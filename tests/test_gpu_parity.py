@@ -434,8 +434,12 @@ def test_capture_paths_matches_oracle(engine, oracle, n_steps, every):
 def test_outline_select_matches_oracle(engine, oracle, shape):
     W, H = shape
     rng = np.random.default_rng(W * 7 + H)
-    for density in (0.0, 0.01, 0.3):
-        e = (rng.random((H, W)) < density).astype(np.float32) * rng.uniform(0.8, 2.0, size=(H, W)).astype(np.float32)
+    for density in (0.0, 0.01, 0.3, -1.0):
+        e = (rng.random((H, W)) < abs(density)).astype(np.float32) * rng.uniform(0.8, 2.0, size=(H, W)).astype(
+            np.float32)
+        if density < 0:  # NaN (never selected), +inf (selected), -inf and a value just below the bar
+            special = np.array([np.nan, np.inf, -np.inf, np.float32(0.8) - np.float32(1e-7)], np.float32)
+            e = special[rng.integers(0, 4, size=(H, W))]
         t = torch.from_numpy(e).cuda()
         pix, pos = engine.outline_select(t, W, H, 0.8)
         o = oracle.outline_select(e, W, H, 0.8)
