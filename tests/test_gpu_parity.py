@@ -60,17 +60,35 @@ def ref_case():
 
 
 def assert_exact(g, o, color_tol=1):
+    """Bit-exact hit ids, step counts and endpoints; a NaN matches a NaN of
+    any sign or payload (CUDA's arithmetic makes 0x7fffffff, the host's
+    0x7fc00000 or its negation; WGSL gives NaNs no bit pattern)."""
     np.testing.assert_array_equal(g["hit_id"], o["hit_id"])
     np.testing.assert_array_equal(g["steps"], o["steps"])
-    np.testing.assert_array_equal(g["mapping"].view(np.uint32), o["mapping"].view(np.uint32))
+    gn, on = np.isnan(g["mapping"]), np.isnan(o["mapping"])
+    np.testing.assert_array_equal(gn, on)
+    np.testing.assert_array_equal(np.where(gn, 0, g["mapping"].view(np.uint32)), np.where(on, 0, o["mapping"].view(np.uint32)))
     assert np.abs(g["color"].astype(int) - o["color"].astype(int)).max() <= color_tol
 
 
+def long_steps_case():
+    """Steps of 0.37 (segments longer than the cell lists reach, so the BVH
+    walk tests them) and of 1.9 (a segment can cross the whole room)."""
+    w = wl.plain_small(80, 60)
+    w.params = wl.fixed_steps(0.37, 12, kahan=False)
+    return w
+
+
 @pytest.mark.parametrize("bvh", [False, True])
-@pytest.mark.parametrize("case", ["steps", "reference"])
+@pytest.mark.parametrize("case", ["steps", "reference", "long_steps", "room_steps"])
 @pytest.mark.parametrize("name", EXACT_FIELDS)
 def test_precise_bit_exact(engine, oracle, name, case, bvh):
-    w = steps_case() if case == "steps" else ref_case()
+    if case in ("long_steps", "room_steps"):
+        w = long_steps_case()
+        if case == "room_steps":
+            w.params = wl.fixed_steps(1.9, 4, kahan=True)
+    else:
+        w = steps_case() if case == "steps" else ref_case()
     engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=bvh)
     g = gpu_render(engine, w, field(engine, name, True))
     o = oracle_render(oracle, w, _abi.FIELD_IDS[name], w.width, w.height)
