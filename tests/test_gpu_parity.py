@@ -377,17 +377,21 @@ def test_render_host_matches_device(engine):
         np.testing.assert_array_equal(d[k], h[k])
 
 
+@pytest.mark.parametrize("name", ["twist", "lens"])
 @pytest.mark.parametrize("size", [(1920, 1080), (640, 417), (513, 1031)])
-def test_render_host_bands_match_device(engine, size):
+def test_render_host_bands_match_device(engine, size, name):
     """Frames of >= 2^18 pixels go to the host in row bands rendered on two
     streams while earlier bands are copied: every plane equals the one-launch
-    device render (band edges at multiples of 16 rows, ragged last band)."""
+    device render (band edges at multiples of 16 rows, ragged last band); the
+    1080p lens frame runs two rays per thread in both."""
     w = wl.frames_1080p(*size)
     w.params = wl.fixed_steps(0.01, 300, kahan=True)
     engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
-    fld = field(engine, "twist", False)
+    fld = field(engine, name, False)
     d = gpu_render(engine, w, fld)
     h = engine.render_host(fld, w.camera, w.settings, w.params, w.width, w.height)
+    if name == "lens" and size == (1920, 1080):
+        assert fld.pair_state() == 1
     for k in d:
         np.testing.assert_array_equal(d[k], h[k])
 
