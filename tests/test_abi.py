@@ -28,6 +28,14 @@ def test_every_declared_symbol_is_exported(lib):
     assert set(names) == set(_abi.PROTOTYPES), set(names) ^ set(_abi.PROTOTYPES)
 
 
+def test_rust_binding_declares_every_function():
+    """The Rust FFI binding a maintainer would add declares
+    exactly the header's functions."""
+    text = (HEADER.parents[1] / "INTEGRATION.md").read_text()
+    rust = sorted(set(re.findall(r"pub fn (linon_[a-z0-9_]+)\(", text)))
+    assert rust == declared_functions(), set(rust) ^ set(declared_functions())
+
+
 def test_constants_match_header():
     """Every LINON_* enum value and #define the Python bindings restate has
     the header's value."""
