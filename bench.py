@@ -376,8 +376,12 @@ def main():
         achieved = fl[i][0] * steps_per_frame[i] / (per_field_ms[i] * 1e-3) / 1e12
         result["roofline"] = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                               "frac": achieved / peak, "traffic": None,
-                              "traffic_note": "DRAM bytes per launch are in profiles/ (ncu); the 58 MB of "
-                                              "output planes are still L2-resident when the launch ends",
+                              "traffic_note": "not measured in this run (ncu cannot run inside it); a separate ncu "
+                                              "capture of the same kernels at 1080p (profiles/"
+                                              "march_1080p_traffic.md) counts 0.60 MB read + 3.36 MB written "
+                                              "per lens launch, 37-39 MB per linear or twist launch: most of "
+                                              "the 58 MB of output planes is still L2-resident when the "
+                                              "launch ends",
                               "kernel": kernel_name(fields[i], ["linear", "twist", "lens"][i]),
                               "peak_source": "measured FFMA probe in this run (linon_probe_fp32_peak)",
                               "peak_nominal_at_median_clock": (n_sm * 128 * 2 * clk["sm_mhz"] * 1e6 / 1e12
