@@ -95,6 +95,32 @@ def test_precise_bit_exact(engine, oracle, name, case, bvh):
     assert_exact(g, o)
 
 
+@pytest.mark.parametrize("weight", [0.0, 1.0, 1.5])
+@pytest.mark.parametrize("view", ["degenerate_up", "from_inside", "grazing"])
+@pytest.mark.parametrize("name", ["lorenz", "translation_x"])
+def test_precise_cameras_and_weights(engine, oracle, name, view, weight):
+    """Field weights 0 (straight rays), 1 (the blend-free kernel variant) and
+    1.5 (extrapolation), with a camera whose up vector is its view direction
+    (the shader's basis is NaN: every ray is NaN), one inside the room, and
+    one grazing the floor; precise module bit-exact to the FP32 oracle."""
+    from linon_gb300 import camera as cam
+    w = wl.plain_small(72, 40)
+    w.params = wl.fixed_steps(0.03, 90, kahan=True)
+    w.settings.field_weight = weight
+    if view == "degenerate_up":
+        w.camera = cam.make_camera((0.0, 3.0, 0.0), (0.0, -1.0, 0.0), (0.0, -1.0, 0.0))
+    elif view == "from_inside":
+        w.camera = cam.make_camera((0.1, -0.2, 0.3), (0.2, 0.3, -0.93), (0.0, 1.0, 0.0))
+    else:
+        w.camera = cam.make_camera((-0.9, -0.999, 0.9), (0.7, 0.0005, -0.7), (0.0, 1.0, 0.0))
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    g = gpu_render(engine, w, field(engine, name, True))
+    o = oracle_render(oracle, w, _abi.FIELD_IDS[name], 72, 40)
+    assert_exact(g, o)
+    if view == "degenerate_up":
+        assert np.isnan(g["mapping"][..., :3]).all()
+
+
 @pytest.mark.parametrize("name", TRANSC_FIELDS)
 def test_precise_transcendental_fields_close(engine, oracle, name):
     w = steps_case()
