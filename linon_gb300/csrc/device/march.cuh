@@ -875,9 +875,18 @@ __device__ __forceinline__ void march_pair_kernel(const F& field, const MarchArg
       dir = vec3p((f2(1.0f) - w) * dir) + v * w;
     }
     const vec3p step_dir = dir * h;
+    // The new position first (with Kahan sums: the compensated sum, which
+    // lies within rounding of p + step_dir); the safe-ball test reads it, so
+    // the segment end is formed only for a lane that is tested.
+    vec3p ky, pn;
+    if (KAHAN) {
+      ky = step_dir - cp;
+      pn = p + ky;
+    } else {
+      pn = p + step_dir;
+    }
     if (!(has0 && has1)) {
-      const vec3p seg_end = p + step_dir;
-      const vec3p dq = seg_end - q0;
+      const vec3p dq = pn - q0;
       const f2 d2 = wgsl::dot(dq, dq);
       const bool need0 = !has0 && !(d2.v.x <= safe2.v.x);
       const bool need1 = !has1 && !(d2.v.y <= safe2.v.y);
@@ -891,8 +900,8 @@ __device__ __forceinline__ void march_pair_kernel(const F& field, const MarchArg
           vec3f q = pair_lane(q0, k);
           float sf = k ? safe2.v.y : safe2.v.x;
           int cool = k ? cool1 : cool0;
-          segment_test<false>(sc, pair_lane(p, k), pair_lane(step_dir, k), pair_lane(seg_end, k), has, color, face, q,
-                              sf, cool, a.err);
+          const vec3f pk = pair_lane(p, k), sk = pair_lane(step_dir, k);
+          segment_test<false>(sc, pk, sk, wgsl::vadd(pk, sk), has, color, face, q, sf, cool, a.err);
           if (has && (k ? in1 : in0)) {  // the first hit decides the pixel's colour and face
             const size_t idx = k ? idx1 : idx0;
             if (a.frame.color) {
@@ -920,12 +929,11 @@ __device__ __forceinline__ void march_pair_kernel(const F& field, const MarchArg
       }
     }
     if (KAHAN) {
-      kahan_add_pair(p.x, cp.x, step_dir.x);
-      kahan_add_pair(p.y, cp.y, step_dir.y);
-      kahan_add_pair(p.z, cp.z, step_dir.z);
+      cp = vec3p(pn - p) - ky;
+      p = pn;
       kahan_add_pair(t, ct, h);
     } else {
-      p = p + step_dir;
+      p = pn;
       t = t + h;
     }
     __syncwarp();
