@@ -1211,11 +1211,23 @@ WG_HD f2 max(f2 a, f2 b) { return f2(fmaxf(a.v.x, b.v.x), fmaxf(a.v.y, b.v.y)); 
 WG_HD f2 clamp(f2 e, f2 lo, f2 hi) { return min(max(e, lo), hi); }
 WG_HD f2 sigmoid(f2 x) { return f2(1.0f) / (f2(1.0f) + exp(neg(x))); }
 WG_HD void sincos2(f2 x, f2* s, f2* c) {
+#if !defined(LINON_PRECISE) && !defined(LINON_SINCOS_POLY) && defined(__CUDA_ARCH__)
+  // sincos_fast's reduction by 2 pi with the multiply and the two FMAs
+  // packed (each lane rounds as the one-ray code does; fma(k, -P, x) is
+  // fma(-k, P, x)), then the special-function unit lane by lane
+  const f2 y = mul2(x, f2(0x1.45f306p-3f));
+  const f2 k(rintf(y.v.x), rintf(y.v.y));
+  f2 r = fma2(k, f2(-0x1.921fb6p+2f), x);
+  r = fma2(k, f2(0x1.777a5cp-23f), r);
+  *s = f2(__sinf(r.v.x), __sinf(r.v.y));
+  *c = f2(__cosf(r.v.x), __cosf(r.v.y));
+#else
   float s0, c0, s1, c1;
   sincos_(x.v.x, &s0, &c0);
   sincos_(x.v.y, &s1, &c1);
   *s = f2(s0, s1);
   *c = f2(c0, c1);
+#endif
 }
 
 typedef vec<f2, 3> vec3p;
