@@ -450,8 +450,9 @@ def test_overlay_matches_oracle(engine, oracle, fp64, srgb):
     assert np.abs(target.cpu().numpy().astype(int) - o_rgba.astype(int)).max() <= 1
 
 
+@pytest.mark.parametrize("fp64,srgb", [(True, False), (False, True)])
 @pytest.mark.parametrize("delta", [1, 9, 10, 30])
-def test_overlay_border_widths_match_oracle(engine, oracle, delta):
+def test_overlay_border_widths_match_oracle(engine, oracle, delta, fp64, srgb):
     """A non-square frame (96x40) with central-difference deltas whose 2*delta
     border leaves a few interior rows (9), none (10: rows 20..19) or covers
     the frame (30); both overlay modes; the exponents buffer is pre-filled
@@ -467,10 +468,11 @@ def test_overlay_border_widths_match_oracle(engine, oracle, delta):
         st = wl.settings(overlay_mode=mode, delta=delta, scaling=50.0)
         target = torch.empty((40, 96, 4), dtype=torch.uint8, device="cuda")
         expo = torch.full((40, 96), -7.0, dtype=torch.float32, device="cuda")
-        engine.overlay(st, 96, 40, color, mapping, target, expo, srgb=False, fp64=True)
+        engine.overlay(st, 96, 40, color, mapping, target, expo, srgb=srgb, fp64=fp64)
         torch.cuda.synchronize()
         o_e = np.full((40, 96), -7.0, np.float32)
-        o_rgba, o_e = oracle.overlay(g["color"], g["mapping"], 96, 40, st, srgb=False, precision=64, exponents=o_e)
+        o_rgba, o_e = oracle.overlay(g["color"], g["mapping"], 96, 40, st, srgb=srgb, precision=64 if fp64 else 32,
+                                     exponents=o_e)
         np.testing.assert_allclose(expo.cpu().numpy(), o_e, rtol=1e-5, atol=1e-6)
         assert np.abs(target.cpu().numpy().astype(int) - o_rgba.astype(int)).max() <= 1
 
