@@ -1,5 +1,6 @@
-"""Serving loop (continuous batching): results alone == results in the mix,
-HBM-budget admission, overlap of waves, bounded waits."""
+"""Serving loop (continuous batching): results alone == results in the mix
+== the drop-in calls' results, HBM-budget admission, overlap of waves,
+bounded waits."""
 import numpy as np
 import pytest
 import torch
@@ -130,6 +131,53 @@ def test_results_alone_equal_results_in_the_mix(engine):
         for k in a:
             np.testing.assert_array_equal(np.asarray(a[k]), np.asarray(b[k]))
     assert all(x["ray_steps"] > 0 for x in alone if "ray_steps" in x)
+
+
+@pytest.mark.gpu
+def test_served_results_equal_the_plain_calls(engine):
+    """Frames, overlays and captures served in shared waves (precise
+    modules) equal, bit for bit, what the drop-in calls give for the same
+    request: linon_render, linon_overlay (linear output) and
+    linon_capture_paths."""
+    from linon_gb300 import FramePlanes
+    fields = _setup(engine, precise=True)
+    reqs = _requests()
+    srv = serving.Server(engine, fields, slots=3)
+    try:
+        ids = [srv.submit(req, pos) for req, pos in reqs]
+        served = []
+        for rid, (req, _) in zip(ids, reqs):
+            srv.wait(rid)
+            served.append(_fetch(srv, rid, req))
+        for rid in ids:
+            srv.release(rid)
+    finally:
+        srv.stop()
+    for (req, pos), s in zip(reqs, served):
+        fld = fields[req.field_index]
+        W, H = req.width, req.height
+        if req.kind == _abi.LINON_REQ_CAPTURE:
+            npts = -(-req.n_steps // req.record_every) + 1
+            out = torch.empty((req.n_rays, npts, 4), dtype=torch.float32, device="cuda")
+            engine.capture_paths(fld, req.camera, req.settings, req.params, W, H, pos, req.h, req.n_steps,
+                                 req.record_every, out)
+            engine.synchronize()
+            np.testing.assert_array_equal(out.cpu().numpy(), s["paths"])
+            continue
+        planes = FramePlanes.allocate(W, H)
+        engine.render(fld, req.camera, req.settings, req.params, planes)
+        engine.synchronize()
+        for k in ("color", "mapping", "hit_id", "steps"):
+            np.testing.assert_array_equal(getattr(planes, k).cpu().numpy().reshape(-1), s[k], err_msg=k)
+        if req.kind == _abi.LINON_REQ_OVERLAY:
+            target = torch.empty((H, W, 4), dtype=torch.uint8, device="cuda")
+            expo = torch.zeros((H, W), dtype=torch.float32, device="cuda")
+            engine.overlay(req.settings, W, H, planes.color, planes.mapping, target, expo, srgb=False,
+                           fp64=bool(req.fp64_overlay))
+            engine.synchronize()
+            np.testing.assert_array_equal(target.cpu().numpy().reshape(-1), s["overlay"])
+            # the served exponents buffer starts zeroed like this one; border pixels stay 0
+            np.testing.assert_array_equal(expo.cpu().numpy().reshape(-1), s["exponents"])
 
 
 @pytest.mark.gpu
