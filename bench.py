@@ -533,7 +533,7 @@ def bench_batch(eng, stream, wl, torch, dev, predefined_source, keep=None):
         views.append(v)
         planes.append(p)
 
-    def timed(fn, reps=3):
+    def timed(fn, reps=5):
         ts = []
         with torch.cuda.stream(stream):
             fn()
