@@ -1206,6 +1206,23 @@ WG_F2_LANES(cos, cos_(x))
 WG_F2_LANES(floor, floorf(x))
 WG_F2_LANES(length, fabsf(x))
 #undef WG_F2_LANES
+// the vector forms, component by component (as the one-ray vec<float, N>
+// forms); the three-component one is not a template, so that an unevaluated
+// product (vs2, below) converts to it
+#define WG_F2_VEC(NAME)                                                            \
+  template <int N> WG_HD vec<f2, N> NAME(const vec<f2, N>& v) {                    \
+    vec<f2, N> r;                                                                  \
+    for (int i = 0; i < N; ++i) r[i] = NAME(v[i]);                                 \
+    return r;                                                                      \
+  }                                                                                \
+  WG_HD vec<f2, 3> NAME(const vec<f2, 3>& v) { return NAME<3>(v); }
+WG_F2_VEC(sqrt)
+WG_F2_VEC(inverseSqrt)
+WG_F2_VEC(exp)
+WG_F2_VEC(sin)
+WG_F2_VEC(cos)
+WG_F2_VEC(floor)
+#undef WG_F2_VEC
 WG_HD f2 min(f2 a, f2 b) { return f2(fminf(a.v.x, b.v.x), fminf(a.v.y, b.v.y)); }
 WG_HD f2 max(f2 a, f2 b) { return f2(fmaxf(a.v.x, b.v.x), fmaxf(a.v.y, b.v.y)); }
 WG_HD f2 clamp(f2 e, f2 lo, f2 hi) { return min(max(e, lo), hi); }
@@ -1257,6 +1274,17 @@ WG_HD vec3p operator-(const vs2& m, const vec3p& a) {
 WG_HD vec3p operator+(const vs2& m, const vs2& n) { return vec3p(m) + n; }
 WG_HD vec3p operator-(const vs2& m, const vs2& n) { return vec3p(m) - n; }
 WG_HD vec3p operator-(const vs2& m) { return vec3p(m.v.x * neg(m.s), m.v.y * neg(m.s), m.v.z * neg(m.s)); }
+// every other operation on an unevaluated product rounds the product first,
+// as the one-ray code rounds s * v before using it
+WG_HD vec3p operator*(const vs2& m, const vec3p& a) { return vec3p(m) * a; }
+WG_HD vec3p operator*(const vec3p& a, const vs2& m) { return a * vec3p(m); }
+WG_HD vec3p operator*(const vs2& m, const vs2& n) { return vec3p(m) * vec3p(n); }
+WG_HD vs2 operator*(const vs2& m, f2 s) { return vec3p(m) * s; }
+WG_HD vs2 operator*(f2 s, const vs2& m) { return s * vec3p(m); }
+WG_HD vs2 operator*(const vs2& m, float s) { return vec3p(m) * s; }
+WG_HD vs2 operator*(float s, const vs2& m) { return s * vec3p(m); }
+WG_HD vec3p operator/(const vs2& m, const vec3p& a) { return vec3p(m) / a; }
+WG_HD vec3p operator/(const vec3p& a, const vs2& m) { return a / vec3p(m); }
 WG_HD vec3p operator/(const vec3p& v, f2 s) { return v * (f2(1.0f) / s); }
 WG_HD vec3p operator/(const vec3p& v, float s) { return v * f2(1.0f / s); }
 WG_HD vec3p operator+(const vec3p& v, float s) { return v + vec3p(f2(s)); }
@@ -1268,6 +1296,12 @@ WG_HD f2 dot_add(const vec3p& a, const vec3p& b, f2 s) {
 }
 WG_HD f2 length(const vec3p& v) { return sqrt(dot(v, v)); }
 WG_HD vec3p normalize(const vec3p& v) { return vec3p(v * rsqrt_ftz2(dot(v, v))); }
+// component-wise abs / min / max / clamp of three-component values, not
+// templates, so that an unevaluated product (vs2) converts to them
+WG_HD vec3p abs(const vec3p& v) { return vec3p(abs(v.x), abs(v.y), abs(v.z)); }
+WG_HD vec3p min(const vec3p& a, const vec3p& b) { return vec3p(min(a.x, b.x), min(a.y, b.y), min(a.z, b.z)); }
+WG_HD vec3p max(const vec3p& a, const vec3p& b) { return vec3p(max(a.x, b.x), max(a.y, b.y), max(a.z, b.z)); }
+WG_HD vec3p clamp(const vec3p& e, const vec3p& lo, const vec3p& hi) { return min(max(e, lo), hi); }
 WG_HD vec3p cross(const vec3p& a, const vec3p& b) {
   return vec3p(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }

@@ -16,7 +16,7 @@ import pytest
 import torch
 
 from linon_gb300 import FramePlanes, _abi, camera as cam, scene, workloads as wl
-from linon_gb300.engine import predefined_source
+from linon_gb300.engine import predefined_source, validate_field
 
 pytestmark = pytest.mark.gpu
 
@@ -895,6 +895,46 @@ def test_main_view_mirror(engine):
     torch.cuda.synchronize()
     assert pos.shape == (8, 2)
     assert mv.texture.shape == (48, 64, 4)
+
+
+PAIR_BUILTIN_BODIES = [
+    # lane-wise builtins of the pair runtime: sin, cos, abs, clamp, exp, sqrt,
+    # inverseSqrt, min, max, floor, length, sigmoid, cross, translate, pow
+    "let w = vec3<f32>(sin(p.x), abs(p.y) - 0.5, clamp(p.z, -0.3, 0.3));\n"
+    "return normalize(v0 + 0.2 * w * exp(-dot(p, p)));",
+    "let r = sqrt(dot(p, p) + 0.25);\n"
+    "let s = max(min(inverseSqrt(r), 1.5), 0.2);\n"
+    "return normalize(v - 0.03 * cross(p, v0) * s + 0.01 * floor(2.0 * p));",
+    "let q = translate(p, 0.1, -0.2, 0.05);\n"
+    "return normalize(v + 0.02 * q * sigmoid(length(q) - 1.0) / pow(dot(q, q) + 0.1, 1.5));",
+    # vector forms on unevaluated products (2.0 * p) and vector sqrt/exp/sin/cos
+    "return normalize(v + 0.02 * abs(2.0 * p) - 0.01 * max(2.0 * p, v0) + 0.01 * min(0.5 * p, v0)\n"
+    "    + 0.01 * clamp(3.0 * p, vec3<f32>(-0.3), vec3<f32>(0.3)) + 0.005 * sqrt(abs(p)) * exp(-p)\n"
+    "    + 0.005 * sin(2.0 * p) * cos(p));",
+]
+
+
+@pytest.mark.parametrize("body", range(len(PAIR_BUILTIN_BODIES)))
+def test_pair_kernel_user_fields_match_one_ray_kernel(engine, body, monkeypatch):
+    """User fields built from the pair runtime's lane-wise builtins, two rays
+    per thread against one ray per thread (fast modules): endpoints within
+    FP32 rounding, hit ids equal but for rounding ties."""
+    src = PAIR_BUILTIN_BODIES[body]
+    w = wl.frames_1080p(161, 97)
+    w.params = wl.fixed_steps(0.005, 600, kahan=True)
+    engine.upload_scene(w.xyz, w.faces, w.face_rgb, bvh=True)
+    fld = engine.compile_field(src)
+    assert "pair form: compiles" in validate_field(src)
+    monkeypatch.setenv("LINON_RAY_PAIRS", "1")
+    g2 = gpu_render(engine, w, fld)
+    assert fld.pair_state() == 1
+    monkeypatch.setenv("LINON_RAY_PAIRS", "0")
+    g1 = gpu_render(engine, w, fld)
+    monkeypatch.delenv("LINON_RAY_PAIRS")
+    same = g2["hit_id"] == g1["hit_id"]
+    assert same.mean() >= 0.995, same.mean()
+    d = np.linalg.norm(g2["mapping"][..., :3].astype(np.float64) - g1["mapping"][..., :3], axis=-1)
+    assert np.percentile(d, 99) <= 1e-4, np.percentile(d, 99)
 
 
 @pytest.mark.parametrize("name", ["linear", "twist", "lens", "lorenz_scaled", "lorenz", "roessler", "translation_x"])
