@@ -1205,7 +1205,15 @@ WG_F2_LANES(sin, sin_(x))
 WG_F2_LANES(cos, cos_(x))
 WG_F2_LANES(floor, floorf(x))
 WG_F2_LANES(length, fabsf(x))
+WG_F2_LANES(tan, tanf(x))
+WG_F2_LANES(log, logf(x))
+WG_F2_LANES(log2, log2f(x))
+WG_F2_LANES(exp2, exp2f(x))
+WG_F2_LANES(fract, x - floorf(x))
+WG_F2_LANES(sign, (x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f)))
 #undef WG_F2_LANES
+WG_HD f2 atan2(f2 a, f2 b) { return f2(atan2f(a.v.x, b.v.x), atan2f(a.v.y, b.v.y)); }
+WG_HD f2 step(f2 e, f2 x) { return f2(x.v.x >= e.v.x ? 1.0f : 0.0f, x.v.y >= e.v.y ? 1.0f : 0.0f); }
 // the vector forms, component by component (as the one-ray vec<float, N>
 // forms); the three-component one is not a template, so that an unevaluated
 // product (vs2, below) converts to it
@@ -1222,6 +1230,12 @@ WG_F2_VEC(exp)
 WG_F2_VEC(sin)
 WG_F2_VEC(cos)
 WG_F2_VEC(floor)
+WG_F2_VEC(tan)
+WG_F2_VEC(log)
+WG_F2_VEC(log2)
+WG_F2_VEC(exp2)
+WG_F2_VEC(fract)
+WG_F2_VEC(sign)
 #undef WG_F2_VEC
 WG_HD f2 min(f2 a, f2 b) { return f2(fminf(a.v.x, b.v.x), fminf(a.v.y, b.v.y)); }
 WG_HD f2 max(f2 a, f2 b) { return f2(fmaxf(a.v.x, b.v.x), fmaxf(a.v.y, b.v.y)); }
@@ -1302,6 +1316,27 @@ WG_HD vec3p abs(const vec3p& v) { return vec3p(abs(v.x), abs(v.y), abs(v.z)); }
 WG_HD vec3p min(const vec3p& a, const vec3p& b) { return vec3p(min(a.x, b.x), min(a.y, b.y), min(a.z, b.z)); }
 WG_HD vec3p max(const vec3p& a, const vec3p& b) { return vec3p(max(a.x, b.x), max(a.y, b.y), max(a.z, b.z)); }
 WG_HD vec3p clamp(const vec3p& e, const vec3p& lo, const vec3p& hi) { return min(max(e, lo), hi); }
+WG_HD vec3p atan2(const vec3p& a, const vec3p& b) { return vec3p(atan2(a.x, b.x), atan2(a.y, b.y), atan2(a.z, b.z)); }
+WG_HD vec3p step(const vec3p& e, const vec3p& x) { return vec3p(step(e.x, x.x), step(e.y, x.y), step(e.z, x.z)); }
+// mix, smoothstep, distance and reflect with the one-ray runtime's formulas
+WG_HD f2 mix(f2 a, f2 b, f2 t) { return fma2(b, t, mul2(a, f2(1.0f) - t)); }
+WG_HD vec3p mix(const vec3p& a, const vec3p& b, f2 t) { return vec3p(a * (f2(1.0f) - t)) + b * t; }
+WG_HD vec3p mix(const vec3p& a, const vec3p& b, const vec3p& t) {
+  return vec3p(mix(a.x, b.x, t.x), mix(a.y, b.y, t.y), mix(a.z, b.z, t.z));
+}
+WG_HD f2 smoothstep(f2 lo, f2 hi, f2 x) {
+  const f2 t = clamp((x - lo) / (hi - lo), f2(0.0f), f2(1.0f));
+  return mul2(mul2(t, t), fma2(f2(-2.0f), t, f2(3.0f)));  // 3 - 2 t contracted, as in the one-ray code
+}
+WG_HD vec3p smoothstep(const vec3p& lo, const vec3p& hi, const vec3p& x) {
+  return vec3p(smoothstep(lo.x, hi.x, x.x), smoothstep(lo.y, hi.y, x.y), smoothstep(lo.z, hi.z, x.z));
+}
+WG_HD f2 distance(const vec3p& a, const vec3p& b) { return length(a - b); }
+WG_HD f2 distance(f2 a, f2 b) { return abs(a - b); }
+WG_HD vec3p reflect(const vec3p& e1, const vec3p& e2) {
+  const f2 d = mul2(f2(2.0f), dot(e2, e1));
+  return e1 - e2 * d;
+}
 WG_HD vec3p cross(const vec3p& a, const vec3p& b) {
   return vec3p(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }

@@ -911,6 +911,13 @@ PAIR_BUILTIN_BODIES = [
     "return normalize(v + 0.02 * abs(2.0 * p) - 0.01 * max(2.0 * p, v0) + 0.01 * min(0.5 * p, v0)\n"
     "    + 0.01 * clamp(3.0 * p, vec3<f32>(-0.3), vec3<f32>(0.3)) + 0.005 * sqrt(abs(p)) * exp(-p)\n"
     "    + 0.005 * sin(2.0 * p) * cos(p));",
+    # mix, distance, fract, sign, tan, log, exp2, atan2, reflect, smoothstep, step
+    "let m = mix(v, v0, 0.25) + 0.01 * mix(p, v0, vec3<f32>(0.3, 0.2, 0.1));\n"
+    "let s = 0.01 * (fract(3.0 * p) + 0.5 * sign(p)) + 0.002 * vec3<f32>(tan(0.3 * p.x), log(1.0 + dot(p, p)),\n"
+    "    exp2(-abs(p.z)));\n"
+    "let r = 0.01 * reflect(p, v0) + 0.01 * smoothstep(vec3<f32>(-1.0), vec3<f32>(1.0), p)\n"
+    "    + 0.005 * step(vec3<f32>(0.1), p) + 0.001 * vec3<f32>(atan2(p.y, p.x + 2.0), distance(p, v0), 0.0);\n"
+    "return normalize(m + s + r);",
 ]
 
 
