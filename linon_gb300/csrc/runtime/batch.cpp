@@ -279,10 +279,10 @@ long long batch_table(const linon_view* views, int n_views, const linon_batch_tu
     b.blocks_x = (v.width + 7) / 8;
     blocks += b.blocks_x * ((v.height + 15) / 16);
     b.m = to_dev(v.settings, v.params);
-    for (int k = 0; k < 3; ++k) {
-      b.cam.o[k] = v.camera.origin[k];
-      b.cam.d[k] = v.camera.view_direction[k];
-      b.cam.u[k] = v.camera.up[k];
+    for (int c = 0; c < 3; ++c) {
+      b.cam.o[c] = v.camera.origin[c];
+      b.cam.d[c] = v.camera.view_direction[c];
+      b.cam.u[c] = v.camera.up[c];
     }
     b.field = v.field_index;
     b.tiles_x = (v.width + t.tile_w - 1) / t.tile_w;
