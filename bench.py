@@ -378,7 +378,7 @@ def main():
                               "frac": achieved / peak, "traffic": None,
                               "traffic_note": "not measured in this run (ncu cannot run inside it); a separate ncu "
                                               "capture of the same kernels at 1080p (profiles/"
-                                              "march_1080p_traffic.md) counts 0.60 MB read + 3.36 MB written "
+                                              "march_1080p_traffic.md) counts 0.10 MB read + 3.55 MB written "
                                               "per lens launch, 37-39 MB per linear or twist launch: most of "
                                               "the 58 MB of output planes is still L2-resident when the "
                                               "launch ends",
