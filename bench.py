@@ -40,7 +40,7 @@ UNIT = "ray-steps/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--no-batch", action="store_true")
@@ -69,23 +69,31 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.lines = []
+        self.lines = []  # (host time of arrival, csv line)
+        self.first = threading.Event()
 
     def start(self):
+        """Starts sampling every 100 ms and returns once the first sample has
+        arrived (at most 3 s), so the sampler is live when the timed region
+        begins."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self.first.wait(timeout=3.0)
         except OSError:
             self.proc = None
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+            self.first.set()
 
-    def stop(self):
+    def stop(self, t_begin: float | None = None, t_end: float | None = None):
+        """Summary of the samples that arrived between t_begin and t_end
+        (host perf_counter; all samples when none fall inside)."""
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -93,9 +101,14 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
+        lines = [ln for t, ln in self.lines
+                 if (t_begin is None or t >= t_begin) and (t_end is None or t <= t_end)]
+        window = "timed region" if lines else "whole sampler run (no sample inside the timed region)"
+        if not lines:
+            lines = [ln for _, ln in self.lines]
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        for line in lines:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 7:
                 continue
@@ -108,7 +121,7 @@ class ClockSampler:
                 if v.lower() in ("active", "1", "yes"):
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "window": window, "interval_ms": 100}
 
 
 def flops_per_step(pyoracle, w, fid):
@@ -234,8 +247,11 @@ def run_reference(args):
     from oracle import pyoracle
     w = wl.frames_1080p(args.width, args.height)
     vals = []
+    # each timed step is a bounded sample (about a minute of CPU work over
+    # all timed steps, 1-6 s each), each warm-up step a 1 s sample
+    budget = max(1.0, min(6.0, 60.0 / max(args.steps, 1)))
     for i in range(args.warmup + args.steps):
-        v, threads, sample = cpu_baseline(pyoracle, w, budget_s=6.0 if i >= args.warmup else 2.0)
+        v, threads, sample = cpu_baseline(pyoracle, w, budget_s=budget if i >= args.warmup else 1.0)
         if i >= args.warmup:
             vals.append(v)
     value = statistics.median(vals)
@@ -315,8 +331,9 @@ def main():
                 fev[k][i][1].record(stream)
             evs[k][1].record(stream)
     torch.cuda.synchronize()
-    wall = time.perf_counter() - t_wall
-    clk = clocks.stop()
+    t_end = time.perf_counter()
+    wall = t_end - t_wall
+    clk = clocks.stop(t_wall, t_end)
     eng.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in evs]
     total_ms = sum(step_ms)

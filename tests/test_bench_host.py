@@ -63,3 +63,36 @@ def test_flops_per_step_counts_live_operations():
         ops, steps = pyoracle.count_ops(e, f, w.camera, w.settings, wl.fixed_steps(0.005, 64, kahan=True),
                                         wl._abi.FIELD_IDS[name], w.width, w.height, pix)
         assert live < ops[0, :4].sum() / steps[0]
+
+
+class _Exited:
+    """Stands in for the nvidia-smi process once its output was read."""
+
+    def terminate(self):
+        pass
+
+    def wait(self, timeout=None):
+        return 0
+
+
+def test_clock_sampler_keeps_the_timed_region():
+    """Only samples that arrived inside the timed region count: the idle
+    clock sampled before it starts does not lower the median, and a throttle
+    reason seen afterwards is not reported; with no sample inside, every
+    sample counts and the summary says so."""
+    c = bench.ClockSampler(0)
+    c.proc = _Exited()
+    row = "{sm}, 2070, 900.0, Not Active, Not Active, Not Active, {cap}"
+    c.lines = [(0.5, row.format(sm=1200, cap="Not Active")),
+               (1.1, row.format(sm=2070, cap="Not Active")),
+               (1.2, row.format(sm=2055, cap="Not Active")),
+               (1.3, row.format(sm=2070, cap="Not Active")),
+               (2.5, row.format(sm=1500, cap="Active"))]
+    got = c.stop(1.0, 2.0)
+    assert got["sm_mhz"] == 2070.0 and got["sm_max_mhz"] == 2070.0
+    assert got["reasons"] == [] and got["samples"] == 3 and got["window"] == "timed region"
+    c2 = bench.ClockSampler(0)
+    c2.proc = _Exited()
+    c2.lines = [(0.5, row.format(sm=2070, cap="Active"))]
+    got = c2.stop(1.0, 2.0)
+    assert got["samples"] == 1 and got["reasons"] == ["sw_power_cap"] and got["window"].startswith("whole")
