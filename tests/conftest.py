@@ -1,5 +1,7 @@
 import os
+import shutil
 import sys
+import tempfile
 from pathlib import Path
 
 import pytest
@@ -8,8 +10,25 @@ ROOT = Path(__file__).resolve().parents[1]
 sys.path.insert(0, str(ROOT))
 
 
+# Files the tests write (host builds of lowered fields, fuzz modules, OBJ
+# files) stay inside the repository, in a git-ignored build folder that each
+# run starts empty.
+SCRATCH = ROOT / "_build" / "tests"
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run with -m gpu)")
+    if not hasattr(config, "workerinput"):  # the controlling process only
+        shutil.rmtree(SCRATCH, ignore_errors=True)
+    SCRATCH.mkdir(parents=True, exist_ok=True)
+    if not config.option.basetemp:
+        config.option.basetemp = str(SCRATCH / ("pytest-" + getattr(config, "workerinput", {}).get("workerid", "main")))
+
+
+def scratch_dir(prefix: str) -> Path:
+    """A fresh directory under the tests' scratch folder."""
+    SCRATCH.mkdir(parents=True, exist_ok=True)
+    return Path(tempfile.mkdtemp(prefix=prefix, dir=SCRATCH))
 
 
 @pytest.fixture(scope="session")

@@ -8,12 +8,12 @@ same order, so every predefined field must agree bit for bit.
 import ctypes as C
 import re
 import subprocess
-import tempfile
 from pathlib import Path
 
 import numpy as np
 import pytest
 
+from conftest import scratch_dir
 from linon_gb300 import _abi, translate_wgsl, validate_field
 from linon_gb300.engine import predefined_source
 
@@ -48,7 +48,7 @@ def host_fields(lib):
     parts.append("      default: return 1; }")
     parts.append("    out[3*i] = r.x; out[3*i+1] = r.y; out[3*i+2] = r.z; }")
     parts.append("  return 0; }")
-    d = Path(tempfile.mkdtemp(prefix="linon_fe_"))
+    d = scratch_dir("linon_fe_")
     src = d / "fields.cpp"
     src.write_text("\n".join(parts))
     so = d / "fields.so"
@@ -211,7 +211,7 @@ def _host_eval(body, x, helpers=None, calls=1):
                      "    linon_user::Private pv; wgsl::vec3f r;",
                      "    for (int c = 0; c < calls; ++c) r = linon_user::field_function(pv, pp, p, v0, v, q[12]);",
                      "    out[3*i] = r.x; out[3*i+1] = r.y; out[3*i+2] = r.z; } }"])
-    d = Path(tempfile.mkdtemp(prefix="linon_fe1_"))
+    d = scratch_dir("linon_fe1_")
     (d / "f.cpp").write_text(src)
     r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-shared", "-fPIC", "-o", str(d / "f.so"),
                         str(d / "f.cpp")], capture_output=True, text=True)
@@ -1255,7 +1255,7 @@ def test_fuzzed_fields_never_crash_and_compile_when_accepted():
         if st == _abi.LINON_OK:
             accepted[out.value] = True
     assert len(accepted) > 50
-    d = Path(tempfile.mkdtemp(prefix="linon_fuzz_"))
+    d = scratch_dir("linon_fuzz_")
     files = []
     for k, code in enumerate(accepted):
         f = d / f"m{k}.cpp"
@@ -1344,7 +1344,7 @@ def test_helper_calls_the_field_function():
                      "  linon_user::Private pv;",
                      "  wgsl::vec3f r = linon_user::u_euler(pv, wgsl::vec3f(1.f, 2.f, 3.f), wgsl::vec3f(0.5f, 0.f, 1.f), 0.25f);",
                      "  out[0] = r.x; out[1] = r.y; out[2] = r.z; out[3] = float(pv.u_n); }"])
-    d = Path(tempfile.mkdtemp(prefix="linon_fe2_"))
+    d = scratch_dir("linon_fe2_")
     (d / "f.cpp").write_text(src)
     r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-shared", "-fPIC", "-o", str(d / "f.so"),
                         str(d / "f.cpp")], capture_output=True, text=True)
