@@ -12,7 +12,7 @@ sys.path.insert(0, str(ROOT))
 
 # Files the tests write (host builds of lowered fields, fuzz modules, OBJ
 # files) stay inside the repository, in a git-ignored build folder that each
-# run starts empty.
+# run starts empty and removes when it ends.
 SCRATCH = ROOT / "_build" / "tests"
 
 
@@ -23,6 +23,11 @@ def pytest_configure(config):
     SCRATCH.mkdir(parents=True, exist_ok=True)
     if not config.option.basetemp:
         config.option.basetemp = str(SCRATCH / ("pytest-" + getattr(config, "workerinput", {}).get("workerid", "main")))
+
+
+def pytest_unconfigure(config):
+    if not hasattr(config, "workerinput"):
+        shutil.rmtree(SCRATCH, ignore_errors=True)
 
 
 def scratch_dir(prefix: str) -> Path:
