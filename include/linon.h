@@ -146,6 +146,10 @@ typedef struct linon_field linon_field;
 
 /* ---- library ------------------------------------------------------------ */
 int linon_abi_version(void);
+/* The reference reports shader errors as Err(wgpu::Error) from
+ * reload_shader (main_view.rs:657-679) and panics on runtime errors
+ * (main_view.rs:675); here every failure is a status code, with its message
+ * kept per thread.                                                          */
 const char* linon_last_error(void);
 const char* linon_status_string(int status);
 /* Source text of a predefined field body (functions.rs:33-128) or NULL. */
@@ -224,7 +228,8 @@ int linon_field_compile(linon_ctx* ctx, const char* field_body,
                         const char* helpers_src, int flags, linon_field** out,
                         char* log, size_t log_cap);
 int linon_field_release(linon_ctx* ctx, linon_field* field);
-/* Counted FP32 operations of one field evaluation (from the front end IR):
+/* No counterpart in the reference (naga exposes no such count).  Counted
+ * FP32 operations of one field evaluation (from the front end IR):
  * arithmetic ops and transcendental calls.                                 */
 int linon_field_flops(const linon_field* field, int32_t* arith, int32_t* transcendental);
 /* The CUDA C the front end generated for the field (for diagnostics).      */
@@ -244,7 +249,8 @@ int linon_field_pair_state(const linon_field* field);
  * success `log` holds the compiler/ptxas report (registers, spills).       */
 int linon_field_validate(const char* field_body, const char* helpers_src, int flags,
                          char* log, size_t log_cap);
-/* Lower WGSL to CUDA C without a context or GPU (front end only).          */
+/* Lower WGSL to CUDA C without a context or GPU (front end only): the
+ * WGSL-to-IR half of create_shader_module, with CUDA C as the output.      */
 int linon_wgsl_translate(const char* field_body, const char* helpers_src,
                          char* out, size_t out_cap, char* log, size_t log_cap);
 
@@ -253,7 +259,8 @@ int linon_wgsl_translate(const char* field_body, const char* helpers_src,
 int linon_render(linon_ctx* ctx, const linon_field* field,
                  const linon_camera* camera, const linon_settings* settings,
                  const linon_march_params* params, const linon_frame* out);
-/* Rows [row0, row1) of the same width x height frame (the primary rays of
+/* No counterpart in the reference (it renders whole frames).
+ * Rows [row0, row1) of the same width x height frame (the primary rays of
  * those rows, stored at their rows of `out`; other rows untouched): one
  * shard of a frame split by rows across GPUs (no exchange; an overlay over
  * a shard renders 2 * central_difference_delta halo rows on each inner
@@ -268,7 +275,10 @@ int linon_render_rows(linon_ctx* ctx, const linon_field* field,
  * glyph visualisation).                                                    */
 int linon_field_eval(linon_ctx* ctx, const linon_field* field, const float* in,
                      float* out, int64_t n);
-/* Same, with host output buffers (copied back; NULL planes are skipped).  */
+/* linon_render with host output buffers (copied back; NULL planes are
+ * skipped).  The reference keeps its frames in textures and never reads
+ * them back; this is the call a host without device memory of its own
+ * makes.                                                                    */
 int linon_render_host(linon_ctx* ctx, const linon_field* field,
                       const linon_camera* camera, const linon_settings* settings,
                       const linon_march_params* params, int32_t width,
@@ -284,8 +294,9 @@ int linon_overlay(linon_ctx* ctx, const linon_settings* settings,
                   int32_t width, int32_t height, const uint8_t* ray_casting,
                   const float* mapping, uint8_t* target, float* exponents,
                   int srgb, int fp64);
-/* Finite-time exponent: ln(max over the 4-neighbourhood of |endpoint
- * difference| / initial direction separation) / T, in FP64.               */
+/* No counterpart in the reference (its overlay is the eigenvalue form
+ * above).  Finite-time exponent: ln(max over the 4-neighbourhood of
+ * |endpoint difference| / initial direction separation) / T, in FP64.      */
 int linon_ftle(linon_ctx* ctx, const linon_camera* camera,
                const linon_march_params* params, int32_t width, int32_t height,
                const float* mapping, float horizon_T, float* exponents);
@@ -346,7 +357,9 @@ int linon_capture_paths_noalloc(linon_ctx* ctx, const linon_field* field,
 int linon_outline_select(linon_ctx* ctx, const float* exponents, int32_t width,
                          int32_t height, float min_exp, int32_t* pix_out,
                          float* pos_out);
-/* Exponent value at the given quantile (0..1) over the interior pixels.   */
+/* Exponent value at the given quantile (0..1) over the interior pixels
+ * (no counterpart in the reference, whose outline uses the fixed threshold
+ * 0.8; the p95 threshold selects the outline pixels of a Lyapunov frame).  */
 int linon_exponent_quantile(linon_ctx* ctx, const float* exponents,
                             int32_t width, int32_t height, int32_t border,
                             double q, float* out);
@@ -355,7 +368,8 @@ int linon_exponent_quantile(linon_ctx* ctx, const float* exponents,
 int linon_outline_indices(uint16_t* out, size_t cap);
 
 /* ---- batched rendering: many views in one launch -----------------------
- * Views of any size, camera, step size and field go into one launch.  The
+ * No counterpart in the reference, which renders one view per
+ * MainView::render (main_view.rs:831-849).  Views of any size, camera, step size and field go into one launch.  The
  * views' pixels are cut into tiles, views with the largest step budget
  * first.  Schedules: one CTA per 8x16-pixel tile of every view, the
  * hardware balancing the CTAs (2, the default); a persistent kernel whose
@@ -394,7 +408,8 @@ int linon_autotune_batch(linon_ctx* ctx, const linon_field* const* fields,
                          double* best_ms);
 
 /* ---- serving: continuous batching of requests ---------------------------
- * A server owns a scheduler thread and the context (do not use the context
+ * No counterpart in the reference, which redraws one view per UI event
+ * (application.rs:492-528).  A server owns a scheduler thread and the context (do not use the context
  * from other threads while it runs).  Requests of any kind and size are
  * queued at submit, admitted in arrival order as their output memory fits the
  * HBM budget, and launched in waves: all frames / Enhance re-renders /
@@ -463,12 +478,12 @@ int linon_serve_stats(linon_server* server, linon_serve_counters* out);
 /* Finishes the waves on the GPU, fails still-queued requests, joins.      */
 int linon_serve_stop(linon_server* server);
 
-/* ---- measurement -------------------------------------------------------
+/* ---- measurement (no counterpart in the reference) ----------------------
  * Measured FP32 throughput of the device (independent FFMA chains on every
  * SM, best of 5 launches timed with CUDA events), in TFLOP/s.             */
 int linon_probe_fp32_peak(linon_ctx* ctx, double* tflops);
 
-/* ---- failure path --------------------------------------------------------
+/* ---- failure path (no counterpart in the reference) ---------------------
  * Runs one CTA that waits, with the march kernels' bounded mbarrier wait, on
  * a barrier that nothing completes (no copy is issued), for at most `polls`
  * polls (1..2^24): the wait runs out, the kernel sets error bit 1 and
