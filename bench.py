@@ -405,6 +405,11 @@ def main():
                                                                if clk.get("sm_mhz") else None),
                               "peak_nominal_formula": f"{n_sm} SMs x 128 FP32 lanes x 2 (FMA) x median SM clock",
                               "flops_definition": "live FP32 operations per ray-step (oracle TraceFloat)",
+                              "executed_note": "not measured in this run; ncu instruction counters of the same "
+                                               "kernels at 1080p (profiles/fp32_executed_ops_batch64_and_1080p_"
+                                               "frames.md) count 17.3 / 82.7 / 152.9 executed FP32 operations "
+                                               "per linear / twist / lens ray-step: the lens kernel 0.60 and "
+                                               "the three frames 0.51 of the FFMA probe",
                               "flops_per_step": {n: round(a, 2) for n, (a, _) in zip(["linear", "twist", "lens"], fl)},
                               "transcendentals_per_step": {n: round(t, 2) for n, (_, t) in
                                                            zip(["linear", "twist", "lens"], fl)},
