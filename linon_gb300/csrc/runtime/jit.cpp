@@ -59,7 +59,7 @@ std::vector<std::string> options(bool precise) {
   }
   if (std::getenv("LINON_JIT_VERBOSE")) o.push_back("--ptxas-options=--verbose");
   // extra NVRTC options (space separated), e.g. "-maxrregcount=64" or
-  // "-DLINON_SINCOS_SFU" (see wgsl_rt.cuh); they are part of the cache key
+  // "-DLINON_SINCOS_POLY" (see wgsl_rt.cuh); they are part of the cache key
   if (const char* extra = std::getenv("LINON_JIT_OPTIONS")) {
     std::istringstream is(extra);
     std::string opt;
