@@ -36,6 +36,73 @@ def test_rust_binding_declares_every_function():
     assert rust == declared_functions(), set(rust) ^ set(declared_functions())
 
 
+_C_TO_RUST = {"float": "f32", "double": "f64", "int32_t": "i32", "uint32_t": "u32", "int64_t": "i64",
+              "uint64_t": "u64", "size_t": "usize", "uint8_t": "u8"}
+
+
+def _c_structs():
+    """Field lists of the header's typedef structs: (name, base type, element
+    count, pointer kind) in declaration order."""
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"typedef struct (linon_\w+) \{(.*?)\} \1;", text, re.S):
+        fields = []
+        for decl in m.group(2).split(";"):
+            decl = decl.strip()
+            if not decl:
+                continue
+            d = re.match(r"(const\s+)?(\w+)\s*(\*?)\s*(.*)", decl)
+            const, base, ptr, names = d.groups()
+            for nm in names.split(","):
+                a = re.match(r"\s*(\w+)\s*(?:\[(\d+)\])?", nm)
+                ty = _C_TO_RUST.get(base, base)
+                kind = ("*const " if const else "*mut ") if ptr else ""
+                fields.append((a.group(1), ty, int(a.group(2) or 1), kind))
+        out[m.group(1)] = fields
+    return out
+
+
+def _rust_structs():
+    text = (HEADER.parents[1] / "INTEGRATION.md").read_text()
+    out = {}
+    for m in re.finditer(r"pub struct (linon_\w+) \{(.*?)\}", text, re.S):
+        body = re.sub(r"//[^\n]*", "", m.group(2))
+        if "_p: [u8; 0]" in body:
+            continue
+        fields = []
+        for f in re.finditer(r"pub (\w+): ([^,]+?)\s*(?:,|$)", body.strip()):
+            ty, n, kind = f.group(2).strip(), 1, ""
+            pm = re.match(r"(\*mut |\*const )(\w+)$", ty)
+            if pm:
+                kind, ty = pm.group(1), pm.group(2)
+            while True:  # [T; N] and [[T; N]; M] flatten to T x N*M
+                am = re.match(r"\[(.*); (\d+)\]$", ty)
+                if not am:
+                    break
+                ty, n = am.group(1).strip(), n * int(am.group(2))
+            fields.append((f.group(1), ty, n, kind))
+        out[m.group(1)] = fields
+    return out
+
+
+def test_rust_structs_match_header():
+    """Every struct of the Rust binding in INTEGRATION.md has the header's
+    fields in the header's order, with the same scalar types, element counts
+    and pointer constness, and its constants have the header's values."""
+    c, rust = _c_structs(), _rust_structs()
+    assert len(c) >= 11 and set(c) == set(rust), set(c) ^ set(rust)
+    for name, fields in c.items():
+        assert rust[name] == fields, (name, rust[name], fields)
+    text = HEADER.read_text()
+    vals = {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(LINON_[A-Z0-9_]+)\s*=\s*(-?\d+)", text)}
+    vals.update({m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+(LINON_[A-Z0-9_]+)\s+(\d+)", text)})
+    consts = re.findall(r"pub const (LINON_[A-Z0-9_]+): \w+ = (-?\d+);",
+                        (HEADER.parents[1] / "INTEGRATION.md").read_text())
+    assert len(consts) >= 15
+    for k, v in consts:
+        assert vals[k] == int(v), k
+
+
 def test_constants_match_header():
     """Every LINON_* enum value and #define the Python bindings restate has
     the header's value."""
