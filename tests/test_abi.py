@@ -103,6 +103,35 @@ def test_rust_structs_match_header():
         assert vals[k] == int(v), k
 
 
+def test_ctypes_structs_match_header():
+    """The Python binding's ctypes structures have the header's fields in the
+    header's order, with the same scalar types and element counts (pointers
+    as void pointers)."""
+    py = {"linon_camera": _abi.Camera, "linon_settings": _abi.Settings, "linon_ray_sample": _abi.RaySample,
+          "linon_march_params": _abi.MarchParams, "linon_frame": _abi.Frame, "linon_view": _abi.View,
+          "linon_batch_tuning": _abi.BatchTuning, "linon_request": _abi.Request,
+          "linon_serve_config": _abi.ServeConfig, "linon_result": _abi.Result,
+          "linon_serve_counters": _abi.ServeStats}
+    names = {v: k for k, v in py.items()}
+    # size_t and uint64_t are one ctypes type on LP64 Linux: compare both as u64
+    scalars = {C.c_float: "f32", C.c_double: "f64", C.c_int32: "i32", C.c_uint32: "u32", C.c_int64: "i64",
+               C.c_uint64: "u64", C.c_size_t: "u64", C.c_uint8: "u8"}
+    c = _c_structs()
+    assert set(py) == set(c)
+    for name, cls in py.items():
+        got = []
+        for fname, ftype in cls._fields_:
+            n = 1
+            while hasattr(ftype, "_length_") and ftype is not C.c_void_p:
+                n, ftype = n * ftype._length_, ftype._type_
+            if ftype is C.c_void_p:
+                got.append((fname, "ptr", n))
+            else:
+                got.append((fname, names.get(ftype) or scalars[ftype], n))
+        want = [(f, "ptr" if kind else ("u64" if ty == "usize" else ty), n) for f, ty, n, kind in c[name]]
+        assert got == want, (name, got, want)
+
+
 def test_constants_match_header():
     """Every LINON_* enum value and #define the Python bindings restate has
     the header's value."""
