@@ -183,6 +183,53 @@ def test_reference_leg_does_not_map_the_engine_library():
     assert r.returncode == 0, r.stderr
 
 
+def test_plain_c_caller(lib):
+    """The header is strict C99 and the library links and answers a plain C
+    program (the host-only entry points; no GPU): the boundary a Rust, Go or
+    C caller binds."""
+    import subprocess
+    from conftest import scratch_dir
+    d = scratch_dir("linon_c_")
+    src = d / "caller.c"
+    src.write_text("""
+#include <stdio.h>
+#include <string.h>
+#include "linon.h"
+_Static_assert(sizeof(linon_camera) == 112, "CameraUniform");
+_Static_assert(sizeof(linon_settings) == 24, "Settings");
+_Static_assert(sizeof(linon_ray_sample) == 32, "RaySample");
+int main(void) {
+  linon_march_params p;
+  memset(&p, 0xff, sizeof p);
+  linon_march_params_reference(&p);
+  char out[4096], log[1024];
+  int st = linon_wgsl_translate("return v0;", NULL, out, sizeof out, log, sizeof log);
+  linon_ctx* ctx = NULL;
+  int bad = linon_create(0, 0, &ctx);
+  printf("%d %.3f %.3f %d %d %d %s|%s\\n", linon_abi_version(), p.h_initial, p.t_max, p.max_steps, st,
+         bad != LINON_OK && ctx == NULL, linon_status_string(LINON_ECOMPILE),
+         linon_predefined_name(LINON_FIELD_LORENZ) ? linon_predefined_name(LINON_FIELD_LORENZ) : "?");
+  return 0;
+}
+""")
+    inc = HEADER.parent
+    libdir = Path(_abi.LIB_PATH).parent
+    exe = d / "caller"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", f"-I{inc}", str(src),
+                        f"-L{libdir}", "-llinon", f"-Wl,-rpath,{libdir}", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120,
+                       env={"CUDA_VISIBLE_DEVICES": "", "PATH": "/usr/bin:/bin"})
+    assert r.returncode == 0, r.stderr[-2000:]
+    ver, h, tmax, steps, st, failed_cleanly, rest = r.stdout.split(" ", 6)
+    assert int(ver) == _abi.load().linon_abi_version()
+    assert (float(h), float(tmax), int(steps)) == (0.1, 5.0, 0)
+    assert int(st) == _abi.LINON_OK and int(failed_cleanly) == 1
+    status, name = rest.strip().split("|")
+    assert status and name == predefined_name(_abi.FIELD_IDS["lorenz"])
+
+
 def test_status_strings_and_predefined(lib):
     assert lib.linon_abi_version() == 2
     assert lib.linon_status_string(_abi.LINON_ECOMPILE) == b"field function compilation failed"
