@@ -5,6 +5,7 @@
     python -m linon_gb300 batch --views 64 --repeat 2 [--plain]
     python -m linon_gb300 lyapunov --width 1024 --height 1024 --repeat 2
     python -m linon_gb300 validate --field lens        # NVRTC report, no GPU
+    python -m linon_gb300 validate --body my_field.wgsl [--helpers my_helpers.wgsl]
 
 Prints one JSON line with the device time per launch (CUDA events).
 """
@@ -113,7 +114,18 @@ def cmd_lyapunov(a):
 
 
 def cmd_validate(a):
-    print(validate_field(predefined_source(_field_id(a.field)), precise=a.precise))
+    """Front end + NVRTC on a predefined field or on a user's field body
+    (and helper functions) read from files, as the reference's shader reload
+    does with an edited file (src/main.rs:206-222, main_view.rs:649-690).
+    A rejected field prints the diagnostics and exits with status 1."""
+    from pathlib import Path
+    body = Path(a.body).read_text() if a.body else predefined_source(_field_id(a.field))
+    helpers = Path(a.helpers).read_text() if a.helpers else None
+    try:
+        print(validate_field(body, helpers, precise=a.precise, batched=a.batched))
+    except _abi.LinonCompileError as e:
+        print(e.message)
+        raise SystemExit(1)
 
 
 def main():
@@ -148,7 +160,10 @@ def main():
     ly.add_argument("--repeat", type=int, default=2)
     v = sub.add_parser("validate")
     v.add_argument("--field", default="twist")
+    v.add_argument("--body", help="file holding a field_function body (instead of --field)")
+    v.add_argument("--helpers", help="file holding WGSL helper functions for the body")
     v.add_argument("--precise", action="store_true")
+    v.add_argument("--batched", action="store_true", help="also compile the batched kernels")
     a = ap.parse_args()
     {"render": cmd_render, "batch": cmd_batch, "lyapunov": cmd_lyapunov, "validate": cmd_validate}[a.cmd](a)
 

@@ -1389,3 +1389,23 @@ def test_pair_form_rejects_a_branch_on_a_value():
     # value for both rays of a thread
     log = validate_field("count = count + 1;\nreturn v0 * f32(count);", helpers="var<private> count: i32;")
     assert "pair form: not available" in log
+
+
+def test_cli_validates_a_users_field_files(tmp_path):
+    """`python -m linon_gb300 validate --body F [--helpers G]`: a user's
+    edited field and helper files go through the front end and NVRTC (the
+    reference's reload of an edited shader, src/main.rs:206-222); a rejected
+    body prints the diagnostics and exits with status 1."""
+    import sys
+    (tmp_path / "body.wgsl").write_text("return rotateY(v0, 0.5 * p.y) + my_shift(p);\n")
+    (tmp_path / "helpers.wgsl").write_text("fn my_shift(q: vec3<f32>) -> vec3<f32> { return 0.01 * q; }\n")
+    (tmp_path / "bad.wgsl").write_text("return q;\n")
+    cmd = [sys.executable, "-m", "linon_gb300", "validate"]
+    r = subprocess.run(cmd + ["--body", str(tmp_path / "body.wgsl"), "--helpers", str(tmp_path / "helpers.wgsl")],
+                       cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "registers" in r.stdout
+    r = subprocess.run(cmd + ["--body", str(tmp_path / "bad.wgsl")], cwd=ROOT, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 1
+    assert "no definition in scope for identifier: 'q'" in r.stdout and "line 1, column 8" in r.stdout
