@@ -1,7 +1,6 @@
 import os
 import shutil
 import sys
-import tempfile
 from pathlib import Path
 
 import pytest
@@ -28,12 +27,6 @@ def pytest_configure(config):
 def pytest_unconfigure(config):
     if not hasattr(config, "workerinput"):
         shutil.rmtree(SCRATCH, ignore_errors=True)
-
-
-def scratch_dir(prefix: str) -> Path:
-    """A fresh directory under the tests' scratch folder."""
-    SCRATCH.mkdir(parents=True, exist_ok=True)
-    return Path(tempfile.mkdtemp(prefix=prefix, dir=SCRATCH))
 
 
 @pytest.fixture(scope="session")

@@ -183,13 +183,12 @@ def test_reference_leg_does_not_map_the_engine_library():
     assert r.returncode == 0, r.stderr
 
 
-def test_plain_c_caller(lib):
+def test_plain_c_caller(lib, tmp_path):
     """The header is strict C99 and the library links and answers a plain C
     program (the host-only entry points; no GPU): the boundary a Rust, Go or
     C caller binds."""
     import subprocess
-    from conftest import scratch_dir
-    d = scratch_dir("linon_c_")
+    d = tmp_path
     src = d / "caller.c"
     src.write_text("""
 #include <stdio.h>

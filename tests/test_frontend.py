@@ -8,18 +8,26 @@ same order, so every predefined field must agree bit for bit.
 import ctypes as C
 import re
 import subprocess
+import tempfile
 from pathlib import Path
 
 import numpy as np
 import pytest
 
-from conftest import scratch_dir
 from linon_gb300 import _abi, translate_wgsl, validate_field
 from linon_gb300.engine import predefined_source
 
 ROOT = Path(__file__).resolve().parents[1]
 RT = ROOT / "linon_gb300" / "csrc" / "device" / "wgsl_rt.cuh"
 EVAL_IDS = [i for i in range(1, _abi.FIELD_COUNT)]
+# host builds of lowered fields go to the tests' scratch folder inside the
+# repository (tests/conftest.py empties it at the start and end of a run)
+SCRATCH = ROOT / "_build" / "tests"
+
+
+def scratch_dir(prefix: str) -> Path:
+    SCRATCH.mkdir(parents=True, exist_ok=True)
+    return Path(tempfile.mkdtemp(prefix=prefix, dir=SCRATCH))
 
 
 def _inputs(n=512, seed=0):
